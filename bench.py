@@ -1,0 +1,440 @@
+"""Benchmark of the GB300 batched big-integer library (one JSON line on rank 0).
+
+Headline workload: plain classical multiplication, 16384 pairs of 8192-bit
+integers (128 u64 limbs) -> 16384-bit full products, uniform seeded limbs.
+A step is one batched multiplication over the whole batch.
+
+  value : products/s with operands resident in HBM; K launches on rotating
+          operand sets whose total (4 x 64 MiB) exceeds the 129 MB L2, timed
+          with CUDA events on the launching stream.
+  e2e   : the same metric through the C ABI's host-buffer call
+          (mi_host_mul_full_u64) from pinned host memory, copies inside the
+          timed region.
+  roofline: the multiplication kernel against the integer-multiply ceiling
+          measured in-process (mi_calib_mul32_peak), in 32x32-bit partial
+          products/s; 65536 partial products per instance.
+  workloads: the other benchmark rows measured in the same run (addition GB/s
+          and %HBM against MEASURED_PEAKS.json, the u32-limb variant).
+  cpu_baseline: the oracle's port of the reference CPU path (GMP mpz_mul via
+          gmpAddMulOnce, all host cores) on a bounded sample.
+
+`--impl reference` times the reference's CPU implementation of the path (the
+oracle's port of gmpAddMulOnce over GMP; the reference's own build cannot run
+on an Arm GPU host) on the same workload with all host threads.
+
+Multi-GPU (torchrun, N>1): every rank multiplies its own batch (instances are
+independent, no collective on the data path); max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "midint-arithmetic_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "add GB/s (%HBM); mul products/s by size, ragged-batched vs plain; p50/p99 ms"
+N_MUL, M_MUL = 16384, 128
+N_ADD, M_ADD = 65536, 64
+L2_BYTES = 129 * 1024 * 1024
+CHECK_N = 256  # instances of the timed batch cross-checked against the CPU baseline
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
+    return ap.parse_args()
+
+
+# --- distributed plumbing ------------------------------------------------------
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_dist(world, local):
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local)
+        dist.init_process_group(backend="nccl")
+    else:
+        torch.cuda.set_device(0)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --- clocks ----------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi sampling (200 ms) of SM clocks and throttle reasons."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# --- CPU baseline (oracle port of the reference CPU path) -------------------------
+
+def cpu_baseline(a: np.ndarray, b: np.ndarray, m: int, budget_s: float, op: str = "mul",
+                 check: np.ndarray | None = None) -> dict:
+    """GMP via the oracle's port of gmpAddMulOnce on all host cores, repeated
+    over growing prefixes of the batch until about budget_s of wall time.
+    With `check` (the GPU's products of the first instances) the first CPU
+    pass is also compared with it, limb for limb."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    threads = os.cpu_count() or 1
+    n = a.size // m
+    a32, b32 = a.view(np.uint32), b.view(np.uint32)
+    m32 = 2 * m
+    out_words = m32 if op == "add" else 2 * m32
+    if oracle.gmp_available():
+        kind_note = "GMP mpz_%s through the oracle's port of gmpAddMulOnce (cuda/helper.h:146-170)" % op
+        run = lambda k: oracle.gmp_batch(op == "add", a32[: k * m32], b32[: k * m32], m32, out_words, threads)
+    else:
+        kind_note = "oracle C restatement (GMP absent on this host)"
+        run = lambda k: oracle.batch_u64(op, a[: k * m], b[: k * m], m, threads)
+    k = min(n, CHECK_N)
+    done, elapsed = 0, 0.0
+    matches = None
+    while elapsed < budget_s:
+        t0 = time.perf_counter()
+        res = run(k)
+        dt = time.perf_counter() - t0
+        if check is not None and matches is None:
+            cpu = np.asarray(res[0] if isinstance(res, tuple) else res).view(np.uint64)[: check.size]
+            matches = bool(np.array_equal(cpu, check))
+        done += k
+        elapsed += dt
+        if dt < budget_s / 8 and k < n:
+            k = min(n, k * 2)
+    out = {"value": done / elapsed, "cores": threads, "kind": "port",
+            "sample": f"{done} instances of the workload (prefixes of the batch, repeated), {elapsed:.1f} s; "
+                      + kind_note}
+    if check is not None:
+        out["matches_gpu_first_instances"] = matches
+    return out
+
+
+# --- GPU measurement helpers -------------------------------------------------------
+
+def time_device(fn, sets: int, steps: int, warmup: int, stream) -> float:
+    """Average ms per step: warm-up, then `steps` calls on rotating sets,
+    bracketed by synchronize + events on the launching stream."""
+    import torch
+
+    for i in range(warmup):
+        fn(i % sets)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        fn(i % sets)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measured_peaks() -> dict:
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def run_ours(args):
+    import torch
+
+    import midint
+    import workloads
+
+    world, rank, local = dist_env()
+    init_dist(world, local)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ctx = midint.Context(torch.cuda.current_device())
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    # --- headline: classical multiplication, device-resident operands ---------
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
+    in_bytes = a.nbytes
+    set_bytes = 2 * in_bytes + 2 * in_bytes
+    sets = max(2, -(-4 * L2_BYTES // set_bytes))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(2 * a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+
+    def mul_step(i):
+        ctx.mul_full(da[i], db[i], dr[i], N_MUL, M_MUL, stream=sp)
+
+    # results of the first instances, checked later in the CPU-baseline leg
+    mul_step(0)
+    torch.cuda.synchronize()
+    got = dr[0][: CHECK_N * 2 * M_MUL].cpu().numpy().view(np.uint64).copy()
+
+    peak_prod = midint.calib_mul32_peak()
+    clocks = ClockSampler(local)
+    barrier(world)
+    clocks.start()
+    time.sleep(0.3)
+    ms = time_device(mul_step, sets, args.steps, args.warmup, stream)
+    clk = clocks.stop()
+    ms = max_over_ranks(world, ms)
+    products_s = world * N_MUL / (ms * 1e-3)
+    prods32_per_inst = (2 * M_MUL) ** 2
+    achieved_prod = N_MUL * prods32_per_inst / (ms * 1e-3)
+
+    # --- e2e through the host-buffer C-ABI call, pinned host memory ------------
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    hr = torch.empty(2 * a.size, dtype=torch.int64).pin_memory()
+    han, hbn, hrn = ha.numpy(), hb.numpy(), hr.numpy()
+    for _ in range(2):
+        ctx.host_mul_full(han, hbn, hrn, N_MUL, M_MUL)
+    barrier(world)
+    e2e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.host_mul_full(han, hbn, hrn, N_MUL, M_MUL)
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / e2e_steps)
+    if not np.array_equal(hrn.view(np.uint64)[: CHECK_N * 2 * M_MUL], got):
+        raise SystemExit("bench: e2e product differs from the device-resident one")
+    e2e = {"value": world * N_MUL / e2e_s, "unit": "products/s", "h2d_bytes_per_step": 2 * in_bytes,
+           "d2h_bytes_per_step": 2 * in_bytes, "ms_per_step": e2e_s * 1e3,
+           "path": "mi_host_mul_full_u64 (pinned host buffers, 2-stream chunked copy/compute overlap)"}
+    del da, db, dr
+    torch.cuda.empty_cache()
+
+    extra = {}
+    if not args.no_extra:
+        extra = secondary_workloads(args, ctx, dev, stream, world, rank)
+
+    out = {
+        "metric": METRIC,
+        "value": products_s,
+        "unit": "products/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 limbs (32x32->64-bit integer multiply-add with carry), exact",
+        "data": "synthetic: seeded splitmix64 limbs (uniform)",
+        "config": {"workload": "plain classical multiplication, 16384 pairs x 8192-bit (128 u64 limbs) -> "
+                               "16384-bit full product", "instances_per_gpu": N_MUL, "limbs_u64": M_MUL,
+                   "parallelism": f"replicas x{world} (independent instances)",
+                   "l2": f"inputs rotate over {sets} operand sets of {set_bytes >> 20} MiB (> 4x L2)"},
+        "roofline": {"bound": "int-mul", "achieved": achieved_prod / 1e9, "peak": peak_prod / 1e9,
+                     "unit": "G 32x32-bit partial products/s", "frac": achieved_prod / peak_prod,
+                     "traffic": None,
+                     "peak_source": "measured in-process: mi_calib_mul32_peak (independent mad.lo.cc/madc.hi.cc "
+                                    "chains, the kernel's own instruction mix)",
+                     "per_unit": f"{prods32_per_inst} partial products per instance"},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "e2e": e2e,
+        "workloads": extra,
+    }
+    if rank == 0:
+        a_cpu, b_cpu = workloads.mul_pairs(n=N_MUL, m=M_MUL)
+        out["cpu_baseline"] = dict(cpu_baseline(a_cpu, b_cpu, M_MUL, args.cpu_seconds, "mul", check=got),
+                                   unit="products/s")
+        print(json.dumps(out))
+        if out["cpu_baseline"].get("matches_gpu_first_instances") is False:
+            raise SystemExit("bench: GPU products differ from the CPU baseline's")
+    ctx.close()
+
+
+def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
+    """Addition (GB/s, %HBM) and the u32-limb multiplication variant."""
+    import torch
+
+    import workloads
+
+    sp = stream.cuda_stream
+    res = {}
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+
+    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=workloads.SEED_BASE + 1000 * rank)
+    set_bytes = 3 * a.nbytes + N_ADD
+    sets = max(2, -(-4 * L2_BYTES // set_bytes))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+        dc = [torch.empty(N_ADD, dtype=torch.uint8, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+
+    def add_step(i):
+        ctx.add(da[i], db[i], dr[i], N_ADD, M_ADD, carry=dc[i], stream=sp)
+
+    steps = max(args.steps, 100)
+    ms = max_over_ranks(world, time_device(add_step, sets, steps, max(args.warmup, 5), stream))
+    algo_bytes = N_ADD * (3 * M_ADD * 8 + 1)
+    gbs = algo_bytes / (ms * 1e-3) / 1e9
+    res["add_4096bit"] = {
+        "config": "plain addition, 65536 pairs x 4096-bit (64 u64 limbs), every 8th pair all-ones + 1; "
+                  "sum mod 2^4096 + carry-out byte",
+        "ms_per_launch": ms, "GB/s": gbs * world, "instances/s": world * N_ADD / (ms * 1e-3),
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": (gbs / hbm) if hbm else None, "traffic": None,
+                     "per_unit": "1537 B per instance (2 x 512 B read, 512 B + 1 B written)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "absent"},
+        "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
+    }
+    del da, db, dr, dc
+
+    # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
+    with torch.cuda.stream(stream):
+        da = torch.from_numpy(a.view(np.int64)).to(dev)
+        db = torch.from_numpy(b.view(np.int64)).to(dev)
+        dr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(world, time_device(
+        lambda i: ctx.mul_full(da, db, dr, N_MUL, 2 * M_MUL, limb_bits=32, stream=sp), 1, 20, 3, stream))
+    res["mul_8192bit_u32limbs"] = {"ms_per_launch": ms, "products/s": world * N_MUL / (ms * 1e-3),
+                                   "note": "operands L2-resident between launches (single set)"}
+    del da, db, dr
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import workloads
+
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL)
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup) * 4)
+    for _ in range(min(args.warmup, 3)):
+        cpu_baseline(a, b, M_MUL, per_step / 4, "mul")
+    vals = []
+    cb = None
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 5))):
+        cb = cpu_baseline(a, b, M_MUL, per_step, "mul")
+        vals.append(cb["value"])
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "products/s",
+        "n_gpus": world,
+        "steps": len(vals),
+        "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / len(vals),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 limbs (GMP mpz_mul)",
+        "data": "synthetic: seeded splitmix64 limbs (uniform)",
+        "config": {"workload": "plain classical multiplication, 16384 pairs x 8192-bit (128 u64 limbs) -> "
+                               "16384-bit full product", "instances_per_gpu": N_MUL, "limbs_u64": M_MUL},
+        "cpu_baseline": dict(cb, value=value, unit="products/s"),
+        "e2e": {"value": value, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

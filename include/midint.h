@@ -1,0 +1,156 @@
+/*
+ * midint.h -- C ABI of the GB300 (sm_103a) batched midsize big-integer library.
+ *
+ * A "batch" is n independent instances stored back to back: instance i of an
+ * operand with `limbs` limbs occupies limbs [i*limbs, (i+1)*limbs), limb 0 is
+ * the least significant one (the layout of the reference's drivers and of its
+ * GMP oracle, cuda/helper.h:116 GMP_ORDER -1).  Limbs are uint64_t (`_u64`
+ * entry points) or uint32_t (`_u32`).
+ *
+ * Every entry point returns an mi_status and never aborts.  Device-pointer
+ * entry points are asynchronous on the given stream (NULL = the context's own
+ * stream) and never allocate; the caller owns every buffer it passes and the
+ * library never frees it.  Host-pointer entry points ("compat" and "host")
+ * copy through device buffers that the context keeps and grows on demand, and
+ * return when the result is in host memory.
+ *
+ * Replaces the reference's kernel drivers in cuda/main.cu (gpuAdd :39-44,
+ * gpuMultiply :221-226, gpuMulFFT :415-420) and the kernels they launch
+ * (baddKer cuda/ker-addition.cu.h:227-260, bmulKerQ
+ * cuda/ker-classic-mul.cu.h:468-498, bmulFFT cuda/ker-fft-mul.cu.h:427-454).
+ * The reference fixes the size as a template parameter; here it is a runtime
+ * argument.
+ */
+#ifndef MIDINT_H
+#define MIDINT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mi_status {
+    MI_OK = 0,
+    MI_EINVAL = 1,   /* null pointer, zero/oversized length, misaligned buffer */
+    MI_ENOMEM = 2,   /* a device or pinned-host allocation failed            */
+    MI_ECUDA = 3,    /* a CUDA runtime call or a kernel launch failed         */
+    MI_ETIMEOUT = 4, /* a bounded device-side wait gave up (no hang)          */
+    MI_ENODEV = 5,   /* no usable CUDA device                                  */
+    MI_ENOTSUP = 6   /* combination of arguments not supported                 */
+} mi_status;
+
+/* Opaque per-device context: resident NTT twiddle tables, staging buffers for
+ * the host-pointer calls, the tuned dispatch table and one CUDA stream. */
+typedef struct mi_ctx_s* mi_ctx;
+
+/* A cudaStream_t passed as a plain pointer (NULL = the context's stream). */
+typedef void* mi_stream;
+
+/* Largest operand length, in u64 limbs, that any single-instance kernel takes
+ * (65536 bits).  u32 entry points accept twice as many limbs. */
+#define MI_MAX_LIMBS_U64 1024u
+
+/* ---------------------------------------------------------------------------
+ * Library / context
+ * ------------------------------------------------------------------------- */
+
+/* Version as 10000*major + 100*minor + patch. */
+int mi_version(void);
+
+/* Static text for a status code. */
+const char* mi_status_string(int status);
+
+/* Detail of the last failure on the calling thread ("" if none). */
+const char* mi_last_error(void);
+
+/* Creates a context on `device` (cudaSetDevice semantics, checked). */
+mi_status mi_ctx_create(int device, mi_ctx* out);
+
+/* Destroys a context, after waiting for its stream. NULL is accepted. */
+mi_status mi_ctx_destroy(mi_ctx ctx);
+
+/* Waits for all work queued on the context's stream. */
+mi_status mi_ctx_synchronize(mi_ctx ctx);
+
+/* The context's own stream, as a cudaStream_t. */
+mi_stream mi_ctx_stream(mi_ctx ctx);
+
+/* ---------------------------------------------------------------------------
+ * Batched addition  r = (a + b) mod 2^(bits*limbs), carry_out[i] = carry bit.
+ * Replaces baddKer<Base,IPB,M,Q> (cuda/ker-addition.cu.h:227-260) as launched
+ * by gpuAdd (cuda/main.cu:39-119).  The reference discards the carry-out;
+ * carry_out may be NULL to do the same.  a, b, r: n*limbs limbs each.
+ * r may alias a or b exactly (in-place), but must not partially overlap.
+ * ------------------------------------------------------------------------- */
+mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                     uint8_t* carry_out, uint32_t n, uint32_t limbs, mi_stream stream);
+mi_status mi_add_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r,
+                     uint8_t* carry_out, uint32_t n, uint32_t limbs, mi_stream stream);
+
+/* Fused six-addition composite r = 6a + 10b (mod 2^(bits*limbs)) with the
+ * reference's chain t1=a+b, t2=2t1, t3=t2+b, t4=2t3, t5=t4+t3, r=t5+b held in
+ * registers.  Replaces a6pb10Ker (cuda/ker-addition.cu.h:266-328). */
+mi_status mi_add6_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                      uint32_t n, uint32_t limbs, mi_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Classical (quadratic) multiplication.
+ * mi_mul_lo_*:   r = a*b mod 2^(bits*limbs)   (n*limbs limbs)  -- the
+ *                reference's bmulKerQ semantics (cuda/ker-classic-mul.cu.h:
+ *                468-498, driven by gpuMultiply cuda/main.cu:221-315).
+ * mi_mul_full_*: r = a*b                      (n*2*limbs limbs).
+ * r must not overlap a or b.
+ * ------------------------------------------------------------------------- */
+mi_status mi_mul_lo_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                        uint32_t n, uint32_t limbs, mi_stream stream);
+mi_status mi_mul_lo_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r,
+                        uint32_t n, uint32_t limbs, mi_stream stream);
+mi_status mi_mul_full_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                          uint32_t n, uint32_t limbs, mi_stream stream);
+mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r,
+                          uint32_t n, uint32_t limbs, mi_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Host-pointer compatibility wrappers with the shapes of the reference's
+ * drivers: synchronous, the context is a lazily created one on the current
+ * device, buffers are caller-owned host memory (pinned or pageable), output
+ * truncated to m limbs exactly as the reference does.
+ *   gpuAdd<Base,m>      cuda/main.cu:39-44
+ *   gpuMultiply<Base,m> cuda/main.cu:221-226
+ * ------------------------------------------------------------------------- */
+mi_status mi_compat_gpuAdd_u64(int num_instances, uint32_t m, const uint64_t* h_as,
+                               const uint64_t* h_bs, uint64_t* h_rs);
+mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_as,
+                               const uint32_t* h_bs, uint32_t* h_rs);
+mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_t* h_as,
+                                    const uint64_t* h_bs, uint64_t* h_rs);
+mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_t* h_as,
+                                    const uint32_t* h_bs, uint32_t* h_rs);
+
+/* ---------------------------------------------------------------------------
+ * Host-buffer end-to-end calls on an explicit context: copy in, compute, copy
+ * out, on the context's stream, pipelined in chunks so that copies overlap the
+ * kernels.  Same semantics as the device-pointer calls above.
+ * ------------------------------------------------------------------------- */
+mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b,
+                          uint64_t* h_r, uint8_t* h_carry, uint32_t n, uint32_t limbs);
+mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b,
+                               uint64_t* h_r, uint32_t n, uint32_t limbs);
+
+/* ---------------------------------------------------------------------------
+ * Calibration: throughput of the integer multiply pipe on this device, in
+ * 32x32-bit partial products per second, measured with independent carry
+ * chains of the instruction mix the multiplication kernels issue
+ * (mad.lo.cc / madc.hi.cc).  The denominator of the multiplication kernels'
+ * roofline.  Counterpart of testBasicOps (cuda/ker-helpers.cu.h:226-317).
+ * iters = 0 picks a default (~tens of ms).  Synchronous; current device.
+ * ------------------------------------------------------------------------- */
+mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s, double* seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MIDINT_H */

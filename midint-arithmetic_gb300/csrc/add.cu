@@ -1,0 +1,241 @@
+// add.cu -- batched big-integer addition by carry-lookahead over thread groups.
+//
+// Counterpart of the reference's baddKer / a6pb10Ker (cuda/ker-addition.cu.h:
+// 227-328).  The reference stages each operand global -> shared -> registers
+// with 8-byte loads (cpGlb2Reg, cuda/ker-helpers.cu.h:121-144) and resolves the
+// carries with a Hillis-Steele scan over volatile shared memory plus four block
+// barriers (cuda/ker-addition.cu.h:88-134).  Here every thread loads its Q
+// limbs straight into registers with 128-bit streaming loads, and the carries
+// of a whole warp are resolved by two ballots and one 64-bit add
+// (mi::group_carry); only integers wider than one warp touch shared memory, one
+// word per warp.
+//
+// Mapping: a group of GS threads (power of two) owns one instance, thread t of
+// the group owns limbs [t*Q, t*Q+Q).  GS*Q >= limbs; limbs beyond the instance
+// are zero and never stored.  A block of max(256, GS) threads holds 256/GS
+// groups and strides over the batch.
+#include <cstdio>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace mi {
+namespace {
+
+template <typename L>
+struct Lim;
+template <>
+struct Lim<uint64_t> {
+    using dev_t = unsigned long long;
+};
+template <>
+struct Lim<uint32_t> {
+    using dev_t = unsigned int;
+};
+
+// Streaming (evict-first) scalar load/store; every input limb is read once.
+template <typename L>
+__device__ __forceinline__ L ld_stream(const L* p) {
+    using D = typename Lim<L>::dev_t;
+    return (L)__ldcs(reinterpret_cast<const D*>(p));
+}
+template <typename L>
+__device__ __forceinline__ void st_stream(L* p, L v) {
+    using D = typename Lim<L>::dev_t;
+    __stcs(reinterpret_cast<D*>(p), (D)v);
+}
+
+template <typename L, int Q>
+__device__ __forceinline__ void unpack16(const uint4& t, L* v) {
+    if constexpr (sizeof(L) == 8) {
+        v[0] = (uint64_t(t.y) << 32) | t.x;
+        v[1] = (uint64_t(t.w) << 32) | t.z;
+    } else {
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+    }
+}
+template <typename L, int Q>
+__device__ __forceinline__ uint4 pack16(const L* v) {
+    uint4 t;
+    if constexpr (sizeof(L) == 8) {
+        t.x = uint32_t(v[0]);
+        t.y = uint32_t(v[0] >> 32);
+        t.z = uint32_t(v[1]);
+        t.w = uint32_t(v[1] >> 32);
+    } else {
+        t.x = v[0];
+        t.y = v[1];
+        t.z = v[2];
+        t.w = v[3];
+    }
+    return t;
+}
+
+// Loads the chunk [start, start+Q) of one instance row, zero beyond m.
+template <typename L, int Q, bool VEC>
+__device__ __forceinline__ void load_chunk(const L* __restrict__ row, uint32_t start, uint32_t m, bool valid,
+                                           L (&v)[Q]) {
+    constexpr int PER = 16 / sizeof(L);
+    if constexpr (VEC) {
+        if (valid && start + Q <= m) {
+            const uint4* p = reinterpret_cast<const uint4*>(row + start);
+#pragma unroll
+            for (int k = 0; k < Q / PER; ++k) {
+                const uint4 t = __ldcs(p + k);
+                unpack16<L, Q>(t, &v[k * PER]);
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = (valid && start + q < m) ? ld_stream(row + start + q) : L(0);
+}
+
+template <typename L, int Q, bool VEC>
+__device__ __forceinline__ void store_chunk(L* __restrict__ row, uint32_t start, uint32_t m, bool valid,
+                                            const L (&v)[Q]) {
+    constexpr int PER = 16 / sizeof(L);
+    if (!valid) return;
+    if constexpr (VEC) {
+        if (start + Q <= m) {
+            uint4* p = reinterpret_cast<uint4*>(row + start);
+#pragma unroll
+            for (int k = 0; k < Q / PER; ++k) __stcs(p + k, pack16<L, Q>(&v[k * PER]));
+            return;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+        if (start + q < m) st_stream(row + start + q, v[q]);
+}
+
+// x + y over the group, result in r; returns the group's carry-out.
+template <typename L, int Q, int GS>
+__device__ __forceinline__ uint32_t group_add(const L (&x)[Q], const L (&y)[Q], L (&r)[Q], uint32_t* scratch) {
+    bool g, p;
+    chunk_add<L, Q>(x, y, r, g, p);
+    uint32_t gc;
+    const uint32_t cin = group_carry<GS>(g, p, 0u, &gc, scratch);
+    chunk_inc<L, Q>(r, cin);
+    return gc;
+}
+
+template <typename L, int Q, int GS, bool VEC, int OP>
+__global__ void __launch_bounds__(GS > 256 ? GS : 256)
+    k_add(const L* __restrict__ a, const L* __restrict__ b, L* __restrict__ r, uint8_t* __restrict__ carry,
+          uint32_t n, uint32_t m) {
+    constexpr int BLOCK = GS > 256 ? GS : 256;
+    constexpr int IPB = BLOCK / GS;
+    __shared__ uint32_t scratch[BLOCK / 32];
+    const uint32_t grp = threadIdx.x / GS;
+    const uint32_t t = threadIdx.x % GS;
+    const uint32_t start = t * Q;
+    const uint64_t stride = uint64_t(gridDim.x) * IPB;
+    // Uniform trip count per block: group_carry synchronises the block for GS > 32.
+    for (uint64_t base = uint64_t(blockIdx.x) * IPB; base < n; base += stride) {
+        const uint64_t inst = base + grp;
+        const bool valid = inst < n;
+        const uint64_t off = valid ? inst * m : 0;
+        L x[Q], y[Q], s[Q];
+        load_chunk<L, Q, VEC>(a + off, start, m, valid, x);
+        load_chunk<L, Q, VEC>(b + off, start, m, valid, y);
+        uint32_t gc;
+        if constexpr (OP == ADD_PLAIN) {
+            gc = group_add<L, Q, GS>(x, y, s, scratch);
+        } else {
+            // 6a + 10b by the chain of a6pb10Ker (cuda/ker-addition.cu.h:304-324).
+            L t1[Q], t2[Q], t3[Q], t4[Q], t5[Q];
+            group_add<L, Q, GS>(x, y, t1, scratch);   // t1 = a + b
+            group_add<L, Q, GS>(t1, t1, t2, scratch); // t2 = 2a + 2b
+            group_add<L, Q, GS>(t2, y, t3, scratch);  // t3 = 2a + 3b
+            group_add<L, Q, GS>(t3, t3, t4, scratch); // t4 = 4a + 6b
+            group_add<L, Q, GS>(t4, t3, t5, scratch); // t5 = 6a + 9b
+            gc = group_add<L, Q, GS>(t5, y, s, scratch); // r = 6a + 10b
+        }
+        store_chunk<L, Q, VEC>(r + off, start, m, valid, s);
+        if (OP == ADD_PLAIN && carry != nullptr && valid) {
+            // The carry-out is the value left at limb position m (a padding
+            // limb of zeros plus the carry), or the group's carry-out when the
+            // instance fills the group exactly.
+            if (m < uint32_t(GS * Q)) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    if (start + q == m) carry[inst] = uint8_t(s[q]);
+            } else if (t == GS - 1) {
+                carry[inst] = uint8_t(gc);
+            }
+        }
+    }
+}
+
+template <typename L, int Q, int GS, bool VEC, int OP>
+mi_status launch_one(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, cudaStream_t st) {
+    constexpr int BLOCK = GS > 256 ? GS : 256;
+    constexpr int IPB = BLOCK / GS;
+    uint64_t blocks = (uint64_t(n) + IPB - 1) / IPB;
+    // Enough blocks for full residency several times over; the kernel strides.
+    const uint64_t cap = uint64_t(sm_count()) * 64;
+    if (blocks > cap) blocks = cap;
+    k_add<L, Q, GS, VEC, OP><<<dim3(uint32_t(blocks)), dim3(BLOCK), 0, st>>>(a, b, r, carry, n, m);
+    MI_CUDA_TRY(cudaGetLastError());
+    return MI_OK;
+}
+
+// Picks (Q, GS) from the limb count; VEC needs 16-byte aligned rows.
+template <typename L, bool VEC, int OP>
+mi_status dispatch(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, cudaStream_t st) {
+    constexpr int QS = 16 / sizeof(L);   // limbs per 128-bit load: 2 (u64) or 4 (u32)
+    if (m <= uint32_t(QS * 32)) {
+        const uint32_t gs = pow2ceil((m + QS - 1) / QS);
+        switch (gs) {
+            case 1: return launch_one<L, QS, 1, VEC, OP>(a, b, r, carry, n, m, st);
+            case 2: return launch_one<L, QS, 2, VEC, OP>(a, b, r, carry, n, m, st);
+            case 4: return launch_one<L, QS, 4, VEC, OP>(a, b, r, carry, n, m, st);
+            case 8: return launch_one<L, QS, 8, VEC, OP>(a, b, r, carry, n, m, st);
+            case 16: return launch_one<L, QS, 16, VEC, OP>(a, b, r, carry, n, m, st);
+            default: return launch_one<L, QS, 32, VEC, OP>(a, b, r, carry, n, m, st);
+        }
+    }
+    constexpr int Q2 = 2 * QS;  // 32 bytes per thread for wide integers
+    if (m <= uint32_t(Q2 * 1024)) {
+        const uint32_t gs = pow2ceil((m + Q2 - 1) / Q2);
+        switch (gs) {
+            case 32: return launch_one<L, Q2, 32, VEC, OP>(a, b, r, carry, n, m, st);
+            case 64: return launch_one<L, Q2, 64, VEC, OP>(a, b, r, carry, n, m, st);
+            case 128: return launch_one<L, Q2, 128, VEC, OP>(a, b, r, carry, n, m, st);
+            case 256: return launch_one<L, Q2, 256, VEC, OP>(a, b, r, carry, n, m, st);
+            case 512: return launch_one<L, Q2, 512, VEC, OP>(a, b, r, carry, n, m, st);
+            default: return launch_one<L, Q2, 1024, VEC, OP>(a, b, r, carry, n, m, st);
+        }
+    }
+    return set_error(MI_EINVAL, "add: %u limbs exceeds the single-group maximum", m);
+}
+
+}  // namespace
+
+mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
+                         uint32_t limbs, int op, cudaStream_t st) {
+    const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (limbs % 2 == 0);
+    if (op == ADD_SIX) {
+        return vec ? dispatch<uint64_t, true, ADD_SIX>(a, b, r, nullptr, n, limbs, st)
+                   : dispatch<uint64_t, false, ADD_SIX>(a, b, r, nullptr, n, limbs, st);
+    }
+    return vec ? dispatch<uint64_t, true, ADD_PLAIN>(a, b, r, carry, n, limbs, st)
+               : dispatch<uint64_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, st);
+}
+
+mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
+                         uint32_t limbs, cudaStream_t st) {
+    // An even number of u32 limbs on 8-byte aligned rows is the same bytes as
+    // half as many u64 limbs, with the same carry-out.
+    if (limbs % 2 == 0 && aligned8(a) && aligned8(b) && aligned8(r))
+        return launch_add_u64(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
+                              reinterpret_cast<uint64_t*>(r), carry, n, limbs / 2, ADD_PLAIN, st);
+    // Odd limb counts (or 4-byte aligned rows) cannot use 128-bit accesses.
+    return dispatch<uint32_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, st);
+}
+
+}  // namespace mi

@@ -1,0 +1,373 @@
+// api.cu -- the C ABI (include/midint.h): contexts, argument checks, status
+// codes, the reference-shaped host-pointer wrappers and the pipelined
+// host-buffer calls.
+//
+// The reference's drivers (cuda/main.cu:39-162, 221-356) allocate, copy, launch
+// on the default stream and ignore every error (gpuAssert prints and returns,
+// cuda/helper.h:13-19).  Here device-pointer calls never allocate, launch on the
+// caller's stream and return a status; only the host-pointer calls move data,
+// through staging buffers the context keeps.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+#include "kernels.h"
+
+struct mi_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // host-pointer pipeline: two streams, each with its own device staging area
+    cudaStream_t pipe[2] = {nullptr, nullptr};
+    void* stage[2] = {nullptr, nullptr};
+    size_t stage_cap = 0;
+    std::mutex mu;  // serialises host-pointer calls on one context
+};
+
+namespace mi {
+
+namespace {
+thread_local char g_err[512] = "";
+}
+
+mi_status set_error(mi_status st, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return st;
+}
+
+mi_status cuda_error(cudaError_t e, const char* what) {
+    const mi_status st = (e == cudaErrorMemoryAllocation)                                   ? MI_ENOMEM
+                         : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
+                            e == cudaErrorInvalidDevice)                                     ? MI_ENODEV
+                                                                                             : MI_ECUDA;
+    return set_error(st, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int sm_count() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cache[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cache[dev] = v;
+    }
+    return cache[dev];
+}
+
+}  // namespace mi
+
+using namespace mi;
+
+namespace {
+
+cudaStream_t pick_stream(mi_ctx ctx, mi_stream s) {
+    if (s != nullptr) return reinterpret_cast<cudaStream_t>(s);
+    return ctx ? ctx->stream : nullptr;
+}
+
+mi_status check_ctx(mi_ctx ctx) {
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    int cur = -1;
+    MI_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != ctx->device) MI_CUDA_TRY(cudaSetDevice(ctx->device));
+    return MI_OK;
+}
+
+mi_status check_batch(const void* a, const void* b, const void* r, uint32_t limbs, uint32_t max_limbs,
+                      const char* op) {
+    if (a == nullptr || b == nullptr || r == nullptr) return set_error(MI_EINVAL, "%s: null buffer", op);
+    if (limbs == 0) return set_error(MI_EINVAL, "%s: zero limbs", op);
+    if (limbs > max_limbs) return set_error(MI_EINVAL, "%s: %u limbs exceeds the maximum %u", op, limbs, max_limbs);
+    return MI_OK;
+}
+
+mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* carry, uint32_t n, uint32_t limbs,
+                  mi_stream stream, int limb_bytes, int op) {
+    const uint32_t maxl = kAddMaxLimbs64 * (8 / limb_bytes);
+    MI_TRY(check_batch(a, b, r, limbs, maxl, op == ADD_SIX ? "add6" : "add"));
+    const size_t bytes = size_t(n) * limbs * limb_bytes;
+    if (partial_overlap(a, bytes, r, bytes) || partial_overlap(b, bytes, r, bytes))
+        return set_error(MI_EINVAL, "add: result partially overlaps an operand");
+    if (carry != nullptr && (any_overlap(carry, n, r, bytes) || any_overlap(carry, n, a, bytes) ||
+                             any_overlap(carry, n, b, bytes)))
+        return set_error(MI_EINVAL, "add: carry_out overlaps a limb buffer");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (limb_bytes == 8)
+        return launch_add_u64(static_cast<const uint64_t*>(a), static_cast<const uint64_t*>(b),
+                              static_cast<uint64_t*>(r), carry, n, limbs, op, st);
+    return launch_add_u32(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
+                          static_cast<uint32_t*>(r), carry, n, limbs, st);
+}
+
+mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n, uint32_t limbs, mi_stream stream,
+                  int limb_bytes, bool full) {
+    const uint32_t maxl = kMulMaxN32 / (limb_bytes / 4);
+    MI_TRY(check_batch(a, b, r, limbs, maxl, full ? "mul_full" : "mul_lo"));
+    const size_t in_bytes = size_t(n) * limbs * limb_bytes;
+    const size_t out_bytes = in_bytes * (full ? 2 : 1);
+    if (n > 0 && (any_overlap(r, out_bytes, a, in_bytes) || any_overlap(r, out_bytes, b, in_bytes)))
+        return set_error(MI_EINVAL, "mul: result overlaps an operand");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    const uint32_t n32 = limbs * uint32_t(limb_bytes / 4);
+    return launch_mul_classic(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
+                              static_cast<uint32_t*>(r), n, n32, full, pick_stream(ctx, stream));
+}
+
+// --- default contexts for the reference-shaped host-pointer wrappers -------
+std::mutex g_default_mu;
+mi_ctx g_default[64] = {};
+
+mi_status default_ctx(mi_ctx* out) {
+    int dev = 0;
+    MI_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(MI_ENODEV, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (g_default[dev] == nullptr) MI_TRY(mi_ctx_create(dev, &g_default[dev]));
+    *out = g_default[dev];
+    return MI_OK;
+}
+
+mi_status ensure_stage(mi_ctx ctx, size_t bytes) {
+    if (bytes <= ctx->stage_cap) return MI_OK;
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+        ctx->stage[i] = nullptr;
+    }
+    ctx->stage_cap = 0;
+    size_t cap = 1;
+    while (cap < bytes) cap <<= 1;
+    for (int i = 0; i < 2; ++i) MI_CUDA_TRY(cudaMalloc(&ctx->stage[i], cap));
+    ctx->stage_cap = cap;
+    return MI_OK;
+}
+
+// Copies a batch through the device in chunks on two streams: while chunk c
+// computes and copies back on one stream, chunk c+1 copies in on the other.
+// `launch(da, db, dr, dcarry, count, stream)` runs the kernel on one chunk.
+template <typename F>
+mi_status host_pipeline(mi_ctx ctx, const void* h_a, const void* h_b, void* h_r, uint8_t* h_carry, uint32_t n,
+                        size_t in_row, size_t out_row, F launch) {
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    // Chunk so that each stream's staging area is at most 64 MiB and there are
+    // at least 4 chunks when the batch is big enough to gain from overlap.
+    const size_t per_inst = 2 * in_row + out_row + (h_carry ? 1 : 0) + 64;
+    uint64_t chunk = (64ull << 20) / per_inst;
+    if (chunk == 0) chunk = 1;
+    if (n >= 64 && chunk > (n + 3) / 4) chunk = (n + 3) / 4;
+    if (chunk > n) chunk = n;
+    const size_t off_b = ((chunk * in_row + 255) / 256) * 256;
+    const size_t off_r = off_b + ((chunk * in_row + 255) / 256) * 256;
+    const size_t off_c = off_r + ((chunk * out_row + 255) / 256) * 256;
+    MI_TRY(ensure_stage(ctx, off_c + chunk + 256));
+    int c = 0;
+    for (uint64_t base = 0; base < n; base += chunk, ++c) {
+        const uint32_t cnt = uint32_t((n - base) < chunk ? (n - base) : chunk);
+        cudaStream_t st = ctx->pipe[c & 1];
+        char* stg = static_cast<char*>(ctx->stage[c & 1]);
+        MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
+                                    cudaMemcpyHostToDevice, st));
+        MI_CUDA_TRY(cudaMemcpyAsync(stg + off_b, static_cast<const char*>(h_b) + base * in_row, cnt * in_row,
+                                    cudaMemcpyHostToDevice, st));
+        MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt,
+                      st));
+        MI_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_r) + base * out_row, stg + off_r, cnt * out_row,
+                                    cudaMemcpyDeviceToHost, st));
+        if (h_carry)
+            MI_CUDA_TRY(cudaMemcpyAsync(h_carry + base, stg + off_c, cnt, cudaMemcpyDeviceToHost, st));
+    }
+    MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[0]));
+    MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[1]));
+    return MI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mi_version(void) { return 100; }
+
+const char* mi_status_string(int status) {
+    switch (status) {
+        case MI_OK: return "MI_OK";
+        case MI_EINVAL: return "MI_EINVAL: invalid argument";
+        case MI_ENOMEM: return "MI_ENOMEM: out of memory";
+        case MI_ECUDA: return "MI_ECUDA: CUDA error";
+        case MI_ETIMEOUT: return "MI_ETIMEOUT: bounded device wait timed out";
+        case MI_ENODEV: return "MI_ENODEV: no usable CUDA device";
+        case MI_ENOTSUP: return "MI_ENOTSUP: not supported";
+        default: return "unknown status";
+    }
+}
+
+const char* mi_last_error(void) { return g_err; }
+
+mi_status mi_ctx_create(int device, mi_ctx* out) {
+    if (out == nullptr) return set_error(MI_EINVAL, "mi_ctx_create: null out");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return set_error(MI_ENODEV, "no CUDA device (%s)", cudaGetErrorName(e));
+    if (device < 0 || device >= count) return set_error(MI_ENODEV, "device %d not present (%d devices)", device, count);
+    MI_CUDA_TRY(cudaSetDevice(device));
+    mi_ctx ctx = new (std::nothrow) mi_ctx_s();
+    if (ctx == nullptr) return set_error(MI_ENOMEM, "mi_ctx_create: host allocation");
+    ctx->device = device;
+    mi_status st = MI_OK;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->pipe[0], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->pipe[1], cudaStreamNonBlocking) != cudaSuccess)
+        st = set_error(MI_ECUDA, "mi_ctx_create: stream creation failed");
+    if (st != MI_OK) {
+        mi_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return MI_OK;
+}
+
+mi_status mi_ctx_destroy(mi_ctx ctx) {
+    if (ctx == nullptr) return MI_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->pipe[i]) {
+            cudaStreamSynchronize(ctx->pipe[i]);
+            cudaStreamDestroy(ctx->pipe[i]);
+        }
+        if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MI_OK;
+}
+
+mi_status mi_ctx_synchronize(mi_ctx ctx) {
+    MI_TRY(check_ctx(ctx));
+    MI_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return MI_OK;
+}
+
+mi_stream mi_ctx_stream(mi_ctx ctx) { return ctx ? reinterpret_cast<mi_stream>(ctx->stream) : nullptr; }
+
+mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry_out, uint32_t n,
+                     uint32_t limbs, mi_stream stream) {
+    return add_any(ctx, a, b, r, carry_out, n, limbs, stream, 8, ADD_PLAIN);
+}
+
+mi_status mi_add_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry_out, uint32_t n,
+                     uint32_t limbs, mi_stream stream) {
+    return add_any(ctx, a, b, r, carry_out, n, limbs, stream, 4, ADD_PLAIN);
+}
+
+mi_status mi_add6_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                      mi_stream stream) {
+    return add_any(ctx, a, b, r, nullptr, n, limbs, stream, 8, ADD_SIX);
+}
+
+mi_status mi_mul_lo_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                        mi_stream stream) {
+    return mul_any(ctx, a, b, r, n, limbs, stream, 8, false);
+}
+mi_status mi_mul_lo_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t limbs,
+                        mi_stream stream) {
+    return mul_any(ctx, a, b, r, n, limbs, stream, 4, false);
+}
+mi_status mi_mul_full_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                          mi_stream stream) {
+    return mul_any(ctx, a, b, r, n, limbs, stream, 8, true);
+}
+mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t limbs,
+                          mi_stream stream) {
+    return mul_any(ctx, a, b, r, n, limbs, stream, 4, true);
+}
+
+// --- reference-shaped host-pointer wrappers ---------------------------------
+
+mi_status mi_compat_gpuAdd_u64(int num_instances, uint32_t m, const uint64_t* h_as, const uint64_t* h_bs,
+                               uint64_t* h_rs) {
+    if (num_instances < 0) return set_error(MI_EINVAL, "gpuAdd: negative num_instances");
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, kAddMaxLimbs64, "gpuAdd"));
+    mi_ctx ctx;
+    MI_TRY(default_ctx(&ctx));
+    return mi_host_add_u64(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), m);
+}
+
+mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_as, const uint32_t* h_bs,
+                               uint32_t* h_rs) {
+    if (num_instances < 0) return set_error(MI_EINVAL, "gpuAdd: negative num_instances");
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, 2 * kAddMaxLimbs64, "gpuAdd"));
+    mi_ctx ctx;
+    MI_TRY(default_ctx(&ctx));
+    const size_t row = size_t(m) * 4;
+    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                             return launch_add_u32(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
+                                                   static_cast<uint32_t*>(dr), nullptr, cnt, m, st);
+                         });
+}
+
+mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_t* h_as, const uint64_t* h_bs,
+                                    uint64_t* h_rs) {
+    if (num_instances < 0) return set_error(MI_EINVAL, "gpuMultiply: negative num_instances");
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, kMulMaxN32 / 2, "gpuMultiply"));
+    mi_ctx ctx;
+    MI_TRY(default_ctx(&ctx));
+    const size_t row = size_t(m) * 8;
+    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                             return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
+                                                       static_cast<uint32_t*>(dr), cnt, 2 * m, false, st);
+                         });
+}
+
+mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_t* h_as, const uint32_t* h_bs,
+                                    uint32_t* h_rs) {
+    if (num_instances < 0) return set_error(MI_EINVAL, "gpuMultiply: negative num_instances");
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, kMulMaxN32, "gpuMultiply"));
+    mi_ctx ctx;
+    MI_TRY(default_ctx(&ctx));
+    const size_t row = size_t(m) * 4;
+    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                             return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
+                                                       static_cast<uint32_t*>(dr), cnt, m, false, st);
+                         });
+}
+
+// --- host-buffer end-to-end calls -------------------------------------------
+
+mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_r, uint8_t* h_carry,
+                          uint32_t n, uint32_t limbs) {
+    MI_TRY(check_batch(h_a, h_b, h_r, limbs, kAddMaxLimbs64, "host_add"));
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    const size_t row = size_t(limbs) * 8;
+    return host_pipeline(ctx, h_a, h_b, h_r, h_carry, n, row, row,
+                         [limbs](void* da, void* db, void* dr, uint8_t* dc, uint32_t cnt, cudaStream_t st) {
+                             return launch_add_u64(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
+                                                   static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, st);
+                         });
+}
+
+mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_r, uint32_t n,
+                               uint32_t limbs) {
+    MI_TRY(check_batch(h_a, h_b, h_r, limbs, kMulMaxN32 / 2, "host_mul_full"));
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    const size_t row = size_t(limbs) * 8;
+    return host_pipeline(ctx, h_a, h_b, h_r, nullptr, n, row, 2 * row,
+                         [limbs](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                             return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
+                                                       static_cast<uint32_t*>(dr), cnt, 2 * limbs, true, st);
+                         });
+}
+
+}  // extern "C"

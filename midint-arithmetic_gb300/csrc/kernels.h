@@ -1,0 +1,31 @@
+// kernels.h -- host launchers of the device kernels (internal to the library).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/midint.h"
+
+namespace mi {
+
+enum AddOp : int { ADD_PLAIN = 0, ADD_SIX = 1 };
+
+// Batched addition on u64 or u32 limbs (op = ADD_PLAIN or ADD_SIX).
+// Arguments are already validated; n > 0, limbs > 0.
+mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
+                         uint32_t limbs, int op, cudaStream_t st);
+mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
+                         uint32_t limbs, cudaStream_t st);
+
+// Classical multiplication on u32 limb views (a u64 buffer with m limbs is a
+// u32 buffer with 2m limbs).  full: r has 2*n32 limbs per instance, else n32.
+mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
+                             bool full, cudaStream_t st);
+
+// Largest u32 limb count the classical kernel takes per instance.
+constexpr uint32_t kMulMaxN32 = 2048;
+// Largest u64 limb count the addition kernels take per instance (one group of
+// at most 1024 threads, 4 limbs each).
+constexpr uint32_t kAddMaxLimbs64 = 4096;
+
+}  // namespace mi

@@ -1,0 +1,66 @@
+"""Seeded synthetic batches with the shapes of the benchmark workloads.
+
+All limbs come from splitmix64 streams (seed -> 64-bit words), so every run,
+here and on any other machine, sees the same integers.  Workloads:
+
+* plain addition: 65536 pairs of 4096-bit integers (64 u64 limbs), uniform,
+  with every 8th pair a worst-case carry chain (A all ones, B = 1);
+* classical multiplication: 16384 pairs of 8192-bit integers (128 u64 limbs ->
+  256-limb product), uniform; the u32 variant is the same bytes as 256 u32 limbs;
+* NTT multiplication: 1024 pairs of 65536-bit integers (1024 u64 limbs),
+  uniform, with every 16th pair all ones (maximal coefficients).
+
+The reference's own generator (ourMkRandom, cuda/helper.h:99-114) builds
+words from glibc rand() and never sets the low bit, so it almost never
+produces long carry chains; the worst-case pairs here are added on purpose.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+SEED_BASE = 0x5EED0000
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    """The first `count` outputs of splitmix64 started at `seed`."""
+    with np.errstate(over="ignore"):
+        x = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + _GOLD * np.arange(1, count + 1, dtype=np.uint64)
+        z = (x ^ (x >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(n: int, m: int, seed: int) -> np.ndarray:
+    return splitmix64(seed, n * m)
+
+
+def add_pairs(n: int = 65536, m: int = 64, seed: int = SEED_BASE + 0, worst_every: int = 8):
+    """Addition workload: (a, b) flat u64 arrays of n*m limbs."""
+    a = uniform(n, m, seed)
+    b = uniform(n, m, seed ^ 0xB0B0B0B0)
+    if worst_every:
+        rows = np.arange(0, n, worst_every)
+        a2, b2 = a.reshape(n, m), b.reshape(n, m)
+        a2[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        b2[rows, :] = 0
+        b2[rows, 0] = 1
+    return a, b
+
+
+def mul_pairs(n: int = 16384, m: int = 128, seed: int = SEED_BASE + 1):
+    """Classical-multiplication workload: uniform (a, b) of n*m u64 limbs."""
+    return uniform(n, m, seed), uniform(n, m, seed ^ 0xB0B0B0B0)
+
+
+def ntt_pairs(n: int = 1024, m: int = 1024, seed: int = SEED_BASE + 2, ones_every: int = 16):
+    """NTT-multiplication workload: uniform, every 16th pair all ones."""
+    a = uniform(n, m, seed)
+    b = uniform(n, m, seed ^ 0xB0B0B0B0)
+    if ones_every:
+        rows = np.arange(0, n, ones_every)
+        a.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        b.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    return a, b
