@@ -8,8 +8,8 @@
  * entry points) or uint32_t (`_u32`).
  *
  * Every entry point returns an mi_status and never aborts.  Device-pointer
- * entry points are asynchronous on the given stream (NULL = the context's own
- * stream) and never allocate; the caller owns every buffer it passes and the
+ * entry points are asynchronous on the given stream (NULL = CUDA's default
+ * stream, mi_ctx_stream(ctx) = the context's own) and never allocate; the caller owns every buffer it passes and the
  * library never frees it.  Host-pointer entry points ("compat" and "host")
  * copy through device buffers that the context keeps and grows on demand, and
  * return when the result is in host memory.
@@ -45,7 +45,7 @@ typedef enum mi_status {
  * the host-pointer calls, the tuned dispatch table and one CUDA stream. */
 typedef struct mi_ctx_s* mi_ctx;
 
-/* A cudaStream_t passed as a plain pointer (NULL = the context's stream). */
+/* A cudaStream_t passed as a plain pointer (NULL = CUDA's default stream). */
 typedef void* mi_stream;
 
 /* Largest operand length, in u64 limbs, that any single-instance kernel takes

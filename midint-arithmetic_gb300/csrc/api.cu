@@ -65,10 +65,9 @@ using namespace mi;
 
 namespace {
 
-cudaStream_t pick_stream(mi_ctx ctx, mi_stream s) {
-    if (s != nullptr) return reinterpret_cast<cudaStream_t>(s);
-    return ctx ? ctx->stream : nullptr;
-}
+// NULL is CUDA's default stream, as everywhere in the CUDA runtime; callers
+// that want the context's own stream pass mi_ctx_stream(ctx).
+cudaStream_t pick_stream(mi_ctx, mi_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 
 mi_status check_ctx(mi_ctx ctx) {
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
