@@ -113,6 +113,21 @@ mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint
                           uint32_t n, uint32_t limbs, mi_stream stream);
 
 /* ---------------------------------------------------------------------------
+ * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 1024: every u64
+ * limb is one digit, three 62-bit primes (the first is the reference's
+ * FftPrime64, 29*2^57+1) carry the convolution, Garner's CRT and the final
+ * carry run in the same kernel.  Replaces bmulFFT<P,M,Q>
+ * (cuda/ker-fft-mul.cu.h:427-454) as launched by gpuMulFFT
+ * (cuda/main.cu:415-520); unlike it, the result is exact at every size.
+ * mi_mul_u64 picks the classical or the NTT kernel by size.
+ * r must not overlap a or b.
+ * ------------------------------------------------------------------------- */
+mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                         uint32_t n, uint32_t limbs, mi_stream stream);
+mi_status mi_mul_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                     uint32_t n, uint32_t limbs, mi_stream stream);
+
+/* ---------------------------------------------------------------------------
  * Host-pointer compatibility wrappers with the shapes of the reference's
  * drivers: synchronous, the context is a lazily created one on the current
  * device, buffers are caller-owned host memory (pinned or pageable), output
@@ -128,6 +143,15 @@ mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_
                                     const uint64_t* h_bs, uint64_t* h_rs);
 mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_t* h_as,
                                     const uint32_t* h_bs, uint32_t* h_rs);
+/* gpuMulFFT<FftPrime32, M> (cuda/main.cu:415-420): M 16-bit digits per
+ * instance in, the low M digits of the product out, packed as u16 digits at
+ * digit offset i*M of the output buffer (its first half; the buffer holds M
+ * u32 words per instance), exactly where the reference's kernel writes them
+ * (cuda/ker-fft-mul.cu.h:451-452).  This is the exact result the reference's
+ * disabled validation expects (cuda/main.cu:598-608).  M must be a multiple
+ * of 4 and at most 4096. */
+mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t* h_as,
+                                  const uint16_t* h_bs, uint32_t* h_rs);
 
 /* ---------------------------------------------------------------------------
  * Host-buffer end-to-end calls on an explicit context: copy in, compute, copy
@@ -148,6 +172,19 @@ mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* 
  * iters = 0 picks a default (~tens of ms).  Synchronous; current device.
  * ------------------------------------------------------------------------- */
 mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s, double* seconds);
+
+/* ---------------------------------------------------------------------------
+ * One NTT on a single prime, run by the same transform code as the
+ * multiplication kernels: conv = 0 gives the forward transform of `a` in
+ * natural order (the reference's fft, cuda/ker-fft-mul.cu.h:304-348), conv = 1
+ * the cyclic convolution of a and b mod p (bmulFFTvalid,
+ * cuda/ker-fft-mul.cu.h:512-554).  p odd < 2^62, g of order 2^two_adicity
+ * (two_adicity >= 11), len a power of two in [8, 2048]; host buffers of len
+ * words; synchronous.  Used to check the transform against the reference's
+ * known answers.
+ * ------------------------------------------------------------------------- */
+mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, uint32_t len, int conv,
+                     const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_out);
 
 #ifdef __cplusplus
 }

@@ -14,10 +14,12 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "ntt_host.h"
 
 struct mi_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
+    mi::NttTables ntt;  // resident twiddles of the three NTT primes
     // host-pointer pipeline: two streams, each with its own device staging area
     cudaStream_t pipe[2] = {nullptr, nullptr};
     void* stage[2] = {nullptr, nullptr};
@@ -119,6 +121,20 @@ mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n,
     return launch_mul_classic(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
                               static_cast<uint32_t*>(r), n, n32, full, pick_stream(ctx, stream));
 }
+
+mi_status mul_ntt(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                  mi_stream stream) {
+    MI_TRY(check_batch(a, b, r, limbs, kNttMaxLimbs, "mul_ntt"));
+    const size_t in_bytes = size_t(n) * limbs * 8;
+    if (n > 0 && (any_overlap(r, 2 * in_bytes, a, in_bytes) || any_overlap(r, 2 * in_bytes, b, in_bytes)))
+        return set_error(MI_EINVAL, "mul_ntt: result overlaps an operand");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    return launch_mul_ntt(a, b, r, n, limbs, ctx->ntt.params, pick_stream(ctx, stream));
+}
+
+// Size at and above which the full product goes through the NTT kernel.
+constexpr uint32_t kNttCrossoverLimbs = 256;
 
 // --- default contexts for the reference-shaped host-pointer wrappers -------
 std::mutex g_default_mu;
@@ -226,6 +242,7 @@ mi_status mi_ctx_create(int device, mi_ctx* out) {
         cudaStreamCreateWithFlags(&ctx->pipe[0], cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->pipe[1], cudaStreamNonBlocking) != cudaSuccess)
         st = set_error(MI_ECUDA, "mi_ctx_create: stream creation failed");
+    if (st == MI_OK) st = ntt_tables_create(&ctx->ntt);
     if (st != MI_OK) {
         mi_ctx_destroy(ctx);
         return st;
@@ -246,6 +263,7 @@ mi_status mi_ctx_destroy(mi_ctx ctx) {
         if (ctx->stage[i]) cudaFree(ctx->stage[i]);
     }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    ntt_tables_destroy(&ctx->ntt);
     delete ctx;
     return MI_OK;
 }
@@ -288,6 +306,17 @@ mi_status mi_mul_full_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint
 mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t limbs,
                           mi_stream stream) {
     return mul_any(ctx, a, b, r, n, limbs, stream, 4, true);
+}
+
+mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                         mi_stream stream) {
+    return mul_ntt(ctx, a, b, r, n, limbs, stream);
+}
+
+mi_status mi_mul_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                     mi_stream stream) {
+    if (limbs >= kNttCrossoverLimbs && limbs <= kNttMaxLimbs) return mul_ntt(ctx, a, b, r, n, limbs, stream);
+    return mul_any(ctx, a, b, r, n, limbs, stream, 8, true);
 }
 
 // --- reference-shaped host-pointer wrappers ---------------------------------
@@ -340,6 +369,25 @@ mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_
                          [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                        static_cast<uint32_t*>(dr), cnt, m, false, st);
+                         });
+}
+
+mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t* h_as, const uint16_t* h_bs,
+                                  uint32_t* h_rs) {
+    if (num_instances < 0) return set_error(MI_EINVAL, "gpuMulFFT: negative num_instances");
+    if (M == 0 || M % 4 != 0 || M / 4 > kNttMaxLimbs)
+        return set_error(MI_EINVAL, "gpuMulFFT: M = %u u16 digits must be a multiple of 4, at most %u", M,
+                         4 * kNttMaxLimbs);
+    if (h_as == nullptr || h_bs == nullptr || h_rs == nullptr) return set_error(MI_EINVAL, "gpuMulFFT: null buffer");
+    mi_ctx ctx;
+    MI_TRY(default_ctx(&ctx));
+    const uint32_t m = M / 4;  // u64 limbs
+    const size_t row = size_t(m) * 8;
+    // the NTT kernel, storing the low M digits (m limbs) of each product
+    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+                         [ctx, m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                             return launch_mul_ntt(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
+                                                   static_cast<uint64_t*>(dr), cnt, m, ctx->ntt.params, st, true);
                          });
 }
 

@@ -1,0 +1,141 @@
+// ntt_host.cu -- host setup of the NTT kernels: constants of the three primes,
+// the resident twiddle tables of a context, and the raw single-prime
+// transform entry point used to check the transform against the reference's
+// known answers.
+//
+// The reference rebuilds and copies its twiddle tables on every driver call
+// (getOmega / mkOmegas, cuda/ker-fft-mul.cu.h:191-211; cuda/main.cu:458-470);
+// here they are built once per context and stay in device memory.
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "ntt_host.h"
+
+namespace mi {
+
+using u128 = unsigned __int128;
+
+uint64_t host_mulmod(uint64_t a, uint64_t b, uint64_t p) { return uint64_t((u128)a * b % p); }
+
+uint64_t host_powmod(uint64_t a, uint64_t e, uint64_t p) {
+    uint64_t r = 1 % p, x = a % p;
+    while (e) {
+        if (e & 1) r = host_mulmod(r, x, p);
+        x = host_mulmod(x, x, p);
+        e >>= 1;
+    }
+    return r;
+}
+
+uint64_t host_invmod(uint64_t a, uint64_t p) { return host_powmod(a, p - 2, p); }
+
+static uint64_t r_mod(uint64_t p) { return uint64_t(((u128)1 << 64) % p); }
+
+void host_twiddles(uint64_t p, uint64_t g, uint32_t s, uint64_t* tw, uint64_t* itw) {
+    const uint64_t w = host_powmod(g, uint64_t(1) << (s - 11), p);  // order 2048
+    const uint64_t wi = host_invmod(w, p);
+    const uint64_t R = r_mod(p);
+    uint64_t acc = R, acci = R;  // w^0 * R
+    for (int e = 0; e < (1 << 11) / 2; ++e) {
+        tw[e] = acc;
+        itw[e] = acci;
+        acc = host_mulmod(acc, w, p);
+        acci = host_mulmod(acci, wi, p);
+    }
+}
+
+mi_status ntt_tables_create(NttTables* T) {
+    constexpr int E = (1 << 11) / 2;
+    std::vector<uint64_t> h(size_t(6) * E);
+    NttMulParams& P = T->params;
+    std::memset(&P, 0, sizeof(P));
+    for (int q = 0; q < 3; ++q) {
+        const uint64_t p = kNttPrimes[q].p;
+        host_twiddles(p, kNttPrimes[q].g, kNttPrimes[q].s, &h[size_t(2 * q) * E], &h[size_t(2 * q + 1) * E]);
+        P.p[q] = p;
+        P.c[q] = uint32_t(p >> 32);
+        const uint64_t R = r_mod(p);
+        P.kb[q] = host_mulmod(R, R, p);
+        for (int lg = 0; lg < 12; ++lg) P.ka_by_lg[q][lg] = host_mulmod(R, host_invmod(uint64_t(1) << lg, p), p);
+    }
+    const uint64_t q0 = kNttPrimes[0].p, q1 = kNttPrimes[1].p, q2 = kNttPrimes[2].p;
+    P.g01 = host_mulmod(host_invmod(q0 % q1, q1), r_mod(q1), q1);
+    P.g02 = host_mulmod(host_invmod(q0 % q2, q2), r_mod(q2), q2);
+    P.g12 = host_mulmod(host_invmod(q1 % q2, q2), r_mod(q2), q2);
+    const u128 q01 = (u128)q0 * q1;
+    P.q01_lo = uint64_t(q01);
+    P.q01_hi = uint64_t(q01 >> 64);
+    MI_CUDA_TRY(cudaMalloc(&T->d_tw, h.size() * sizeof(uint64_t)));
+    MI_CUDA_TRY(cudaMemcpy(T->d_tw, h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    for (int q = 0; q < 3; ++q) {
+        P.tw[q] = T->d_tw + size_t(2 * q) * E;
+        P.itw[q] = T->d_tw + size_t(2 * q + 1) * E;
+    }
+    return MI_OK;
+}
+
+void ntt_tables_destroy(NttTables* T) {
+    if (T->d_tw) cudaFree(T->d_tw);
+    T->d_tw = nullptr;
+}
+
+}  // namespace mi
+
+using namespace mi;
+
+extern "C" mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, uint32_t len, int conv,
+                                const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_out) {
+    if (h_a == nullptr || h_out == nullptr || (conv && h_b == nullptr)) return set_error(MI_EINVAL, "ntt_raw: null");
+    if (len < 8 || len > 2048 || (len & (len - 1))) return set_error(MI_EINVAL, "ntt_raw: bad length %u", len);
+    if ((p & 1) == 0 || p >= (uint64_t(1) << 62) || two_adicity < 11 || two_adicity > 63)
+        return set_error(MI_EINVAL, "ntt_raw: prime must be odd, < 2^62, with 2-adicity >= 11");
+    constexpr int E = (1 << 11) / 2;
+    std::vector<uint64_t> tw(2 * E);
+    host_twiddles(p, g, two_adicity, tw.data(), tw.data() + E);
+    NttRawArgs A{};
+    A.p = p;
+    A.len = len;
+    A.conv = conv;
+    A.generic = (p & 0xffffffffull) != 1;
+    if (A.generic) {
+        uint32_t inv = 1;  // p^-1 mod 2^32 by Newton iteration
+        for (int i = 0; i < 5; ++i) inv *= 2 - uint32_t(p) * inv;
+        A.aux = uint32_t(0u - inv);
+    } else {
+        A.aux = uint32_t(p >> 32);
+    }
+    const uint64_t R = uint64_t(((unsigned __int128)1 << 64) % p);
+    A.r2 = host_mulmod(R, R, p);
+    A.linv_r = host_mulmod(host_invmod(len, p), R, p);
+    uint64_t* d = nullptr;
+    MI_CUDA_TRY(cudaMalloc(&d, sizeof(uint64_t) * (2 * E + 3 * size_t(len))));
+    mi_status st = MI_OK;
+    uint64_t* da = d + 2 * E;
+    uint64_t* db = da + len;
+    uint64_t* dout = db + len;
+    std::vector<uint64_t> ha(len), hb(len, 0);
+    for (uint32_t i = 0; i < len; ++i) ha[i] = h_a[i] % p;
+    if (conv)
+        for (uint32_t i = 0; i < len; ++i) hb[i] = h_b[i] % p;
+    cudaError_t e = cudaMemcpy(d, tw.data(), sizeof(uint64_t) * 2 * E, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(da, ha.data(), sizeof(uint64_t) * len, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, hb.data(), sizeof(uint64_t) * len, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        st = cuda_error(e, "ntt_raw copy-in");
+    } else {
+        A.a = da;
+        A.b = db;
+        A.out = dout;
+        A.tw = d;
+        A.itw = d + E;
+        st = launch_ntt_raw(A, nullptr);
+        if (st == MI_OK) {
+            e = cudaMemcpy(h_out, dout, sizeof(uint64_t) * len, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) st = cuda_error(e, "ntt_raw copy-out");
+        }
+    }
+    cudaFree(d);
+    return st;
+}

@@ -54,6 +54,10 @@ SIGNATURES = {
     "mi_host_add_u64": (_S, [_P, _P, _P, _P, _P, _U32, _U32]),
     "mi_host_mul_full_u64": (_S, [_P, _P, _P, _P, _U32, _U32]),
     "mi_calib_mul32_peak": (_S, [_U32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "mi_mul_ntt_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
+    "mi_mul_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
+    "mi_compat_gpuMulFFT_u16": (_S, [_I, _U32, _P, _P, _P]),
+    "mi_ntt_raw": (_S, [ctypes.c_uint64, ctypes.c_uint64, _U32, _U32, _I, _P, _P, _P]),
 }
 
 
@@ -153,6 +157,14 @@ class Context:
         f = load().mi_mul_full_u64 if limb_bits == 64 else load().mi_mul_full_u32
         check(f(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
 
+    def mul_ntt(self, a, b, r, n: int, limbs: int, stream=None) -> None:
+        """Exact full product by NTT (u64 limbs, limbs <= 1024)."""
+        check(load().mi_mul_ntt_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
+
+    def mul(self, a, b, r, n: int, limbs: int, stream=None) -> None:
+        """Full product, classical or NTT by size (u64 limbs)."""
+        check(load().mi_mul_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
+
     # --- host-buffer end-to-end calls --------------------------------------
     def host_add(self, h_a: np.ndarray, h_b: np.ndarray, h_r: np.ndarray, h_carry: np.ndarray | None,
                  n: int, limbs: int) -> None:
@@ -167,6 +179,16 @@ def calib_mul32_peak(iters: int = 0) -> float:
     v, t = ctypes.c_double(), ctypes.c_double()
     check(load().mi_calib_mul32_peak(iters, ctypes.byref(v), ctypes.byref(t)))
     return v.value
+
+
+def ntt_raw(p: int, g: int, two_adicity: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:
+    """Forward NTT of `a` (natural order) or, with `b`, the cyclic convolution
+    of a and b mod p, computed on the GPU by the library's transform code."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    out = np.empty_like(a)
+    bb = None if b is None else np.ascontiguousarray(b, dtype=np.uint64)
+    check(load().mi_ntt_raw(p, g, two_adicity, a.size, 0 if b is None else 1, _ptr(a), _ptr(bb), _ptr(out)))
+    return out
 
 
 # --- reference-shaped drivers --------------------------------------------------
@@ -198,6 +220,28 @@ def gpuAdd(Base, m: int, num_instances: int, h_as: np.ndarray, h_bs: np.ndarray,
     _host_args(Base, m, num_instances, (h_as, h_bs, h_rs))
     f = load().mi_compat_gpuAdd_u64 if Base.bits == 64 else load().mi_compat_gpuAdd_u32
     check(f(num_instances, m, _ptr(h_as), _ptr(h_bs), _ptr(h_rs)))
+
+
+class FftPrime32:
+    """The reference's 32-bit NTT prime traits (cuda/ker-fft-mul.cu.h:59-72)."""
+    uhlf_t = np.uint16
+    uint_t = np.uint32
+    p, g, n = 3221225473, 13, 30
+
+
+def gpuMulFFT(P, m: int, num_instances: int, h_as: np.ndarray, h_bs: np.ndarray, h_rs: np.ndarray) -> None:
+    """gpuMulFFT<FftPrime32, m>(num_instances, h_as, h_bs, h_rs): m u16 digits
+    per instance; the low m digits of each product are packed as u16 digits at
+    digit offset i*m of h_rs (whose size is m u32 words per instance), as in the
+    reference's kernel.  Exact, unlike the reference's."""
+    if P is not FftPrime32:
+        raise MidintError(MI_ENOTSUP, "only the FftPrime32 (u16 digit) shape is provided")
+    for x, dt in ((h_as, np.uint16), (h_bs, np.uint16), (h_rs, np.uint32)):
+        if not isinstance(x, np.ndarray) or x.dtype != dt or not x.flags.c_contiguous:
+            raise MidintError(MI_EINVAL, "expected C-contiguous uint16 inputs and a uint32 output")
+    if h_as.size < num_instances * m or h_bs.size < num_instances * m or h_rs.size < num_instances * m:
+        raise MidintError(MI_EINVAL, "arrays too short")
+    check(load().mi_compat_gpuMulFFT_u16(num_instances, m, _ptr(h_as), _ptr(h_bs), _ptr(h_rs)))
 
 
 def gpuMultiply(Base, m: int, num_instances: int, h_as: np.ndarray, h_bs: np.ndarray, h_rs: np.ndarray) -> None:
