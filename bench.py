@@ -333,9 +333,10 @@ def run_ours(args):
 
 
 def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
-    """Addition (GB/s, %HBM) and the u32-limb multiplication variant."""
+    """Addition (GB/s, %HBM), NTT multiplication and the u32-limb variant."""
     import torch
 
+    import midint
     import workloads
 
     sp = stream.cuda_stream
@@ -371,6 +372,35 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
     }
     del da, db, dr, dc
+
+    # NTT multiplication: 1024 pairs x 65536-bit, every 16th pair all ones
+    n_ntt, m_ntt = 1024, 1024
+    a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, seed=workloads.SEED_BASE + 2 + 1000 * rank)
+    set_bytes = 4 * a.nbytes
+    sets = max(2, -(-4 * L2_BYTES // set_bytes))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(2 * a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+    ms = max_over_ranks(world, time_device(
+        lambda i: ctx.mul_ntt(da[i], db[i], dr[i], n_ntt, m_ntt, stream=sp), sets, max(10, args.steps // 2),
+        max(3, args.warmup), stream))
+    peak = midint.calib_mul32_peak()
+    modmuls = 107520          # 3 primes x (3 transforms x 1024*11 butterflies + 2048 pointwise)
+    pp_per_modmul = 6         # 4 partial products for x*y, 2 for the reduction (p = c*2^32 + 1)
+    achieved = n_ntt * modmuls * pp_per_modmul / (ms * 1e-3)
+    res["ntt_mul_65536bit"] = {
+        "config": "plain NTT multiplication, 1024 pairs x 65536-bit (1024 u64 limbs) -> 131072-bit product, "
+                  "every 16th pair all-ones; 3 primes < 2^62, 2048-point transforms, CRT + carry fused",
+        "ms_per_launch": ms, "products/s": world * n_ntt / (ms * 1e-3),
+        "roofline": {"bound": "int-mul", "achieved": achieved / 1e9, "peak": peak / 1e9,
+                     "unit": "G 32x32-bit partial products/s", "frac": achieved / peak,
+                     "per_unit": f"{modmuls} modular multiplies x {pp_per_modmul} partial products per instance",
+                     "peak_source": "mi_calib_mul32_peak (measured in-process)"},
+        "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
+    }
+    del da, db, dr
 
     # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
     a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)

@@ -112,12 +112,36 @@ __device__ __forceinline__ void subc(uint32_t& d, uint32_t a) {
 // GS > 32 every thread of the block must call this (it synchronises the
 // block) and `scratch` must hold (blockDim.x/32) words.
 // ---------------------------------------------------------------------------
+// Lanes of the calling thread's group of GS <= 32 lanes (all 32 for GS = 32).
+template <int GS>
+__device__ __forceinline__ uint32_t group_lanes() {
+    static_assert(GS <= 32, "sub-warp groups only");
+    if constexpr (GS == 32) {
+        return MI_FULL_MASK;
+    } else {
+        const uint32_t lane = threadIdx.x & 31u;
+        return ((1u << GS) - 1u) << (lane & ~uint32_t(GS - 1));
+    }
+}
+
+// Barrier over the group: its own lanes for groups within a warp (so groups
+// of one warp may run different loops), the whole block otherwise.
+template <int GS>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (GS <= 32)
+        __syncwarp(group_lanes<GS>());
+    else
+        __syncthreads();
+}
+
 template <int GS>
 __device__ __forceinline__ uint32_t group_carry(bool g, bool p, uint32_t cin0, uint32_t* gcarry,
                                                 uint32_t* scratch) {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t G = __ballot_sync(MI_FULL_MASK, g);
-    const uint32_t P = __ballot_sync(MI_FULL_MASK, p);
+    uint32_t vote = MI_FULL_MASK;
+    if constexpr (GS <= 32) vote = group_lanes<GS>();
+    const uint32_t G = __ballot_sync(vote, g);
+    const uint32_t P = __ballot_sync(vote, p);
     if constexpr (GS <= 32) {
         const uint32_t base = lane & ~uint32_t(GS - 1);
         const uint64_t mask = (GS == 32) ? 0xffffffffull : ((1ull << GS) - 1ull);

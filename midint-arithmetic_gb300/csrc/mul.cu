@@ -37,39 +37,63 @@ namespace {
 
 constexpr int kT = 8;  // tile side, in 32-bit limbs
 
+// Accumulator of one anti-diagonal of T x T tiles, split by column parity so
+// that every (lo, hi) word pair of a partial product lands on an even-aligned
+// register pair (which lets the compiler issue mad.lo.cc + madc.hi.cc as one
+// wide multiply-add) and each tile row is two independent carry chains:
+//   a[c]   column c,   products with i+j even (chains start at even columns)
+//   b[k]   column k+1, products with i+j odd
+//   cc[c]  carries out of the chains, at column T+c
 template <int T>
-__device__ __forceinline__ void tile_mac(const uint32_t (&A)[T], const uint32_t (&B)[T], uint32_t (&acc)[2 * T + 1],
-                                         uint32_t (&cc)[T + 1]) {
+struct DiagAcc {
+    uint32_t a[2 * T];
+    uint32_t b[2 * T - 2];
+    uint32_t cc[T + 1];
+    static constexpr int WORDS = 2 * T + 2 * T - 2 + T + 1;
+};
+
+template <int T>
+__device__ __forceinline__ void tile_mac(const uint32_t (&A)[T], const uint32_t (&B)[T], DiagAcc<T>& s) {
 #pragma unroll
     for (int i = 0; i < T; ++i) {
-        // even j: columns i .. i+T-1, carry into column i+T
-        mad_lo_cc(acc[i], A[i], B[0]);
-        madc_hi_cc(acc[i + 1], A[i], B[0]);
+        const int j0 = i & 1;  // first j with i+j even: columns i+j0 .. i+j0+T-1
+        mad_lo_cc(s.a[i + j0], A[i], B[j0]);
+        madc_hi_cc(s.a[i + j0 + 1], A[i], B[j0]);
 #pragma unroll
-        for (int j = 2; j < T; j += 2) {
-            madc_lo_cc(acc[i + j], A[i], B[j]);
-            madc_hi_cc(acc[i + j + 1], A[i], B[j]);
+        for (int j = j0 + 2; j < T; j += 2) {
+            madc_lo_cc(s.a[i + j], A[i], B[j]);
+            madc_hi_cc(s.a[i + j + 1], A[i], B[j]);
         }
-        addc(cc[i], 0u);
-        // odd j: columns i+1 .. i+T, carry into column i+T+1
-        mad_lo_cc(acc[i + 1], A[i], B[1]);
-        madc_hi_cc(acc[i + 2], A[i], B[1]);
+        addc(s.cc[i + j0], 0u);
+        const int j1 = 1 - j0;  // first j with i+j odd: columns i+j1 .. i+j1+T-1
+        mad_lo_cc(s.b[i + j1 - 1], A[i], B[j1]);
+        madc_hi_cc(s.b[i + j1], A[i], B[j1]);
 #pragma unroll
-        for (int j = 3; j < T; j += 2) {
-            madc_lo_cc(acc[i + j], A[i], B[j]);
-            madc_hi_cc(acc[i + j + 1], A[i], B[j]);
+        for (int j = j1 + 2; j < T; j += 2) {
+            madc_lo_cc(s.b[i + j - 1], A[i], B[j]);
+            madc_hi_cc(s.b[i + j], A[i], B[j]);
         }
-        addc(cc[i + 1], 0u);
+        addc(s.cc[i + j1], 0u);
     }
 }
 
-// acc[T..2T] += cc[0..T]; the true value always fits in 2T+1 words.
+// The (2T+1)-word value a + b*2^32 + cc*2^(32T) of an accumulator; the true
+// value of an anti-diagonal of at most 2^31 tiles always fits.
 template <int T>
-__device__ __forceinline__ void fold_counters(uint32_t (&acc)[2 * T + 1], const uint32_t (&cc)[T + 1]) {
-    add_cc(acc[T], cc[0]);
+__device__ __forceinline__ void fold(const uint32_t* a, const uint32_t* b, const uint32_t* cc,
+                                     uint32_t (&f)[2 * T + 1]) {
 #pragma unroll
-    for (int c = 1; c < T; ++c) addc_cc(acc[T + c], cc[c]);
-    addc(acc[2 * T], cc[T]);
+    for (int c = 0; c < 2 * T; ++c) f[c] = a[c];
+    f[2 * T] = 0;
+    add_cc(f[1], b[0]);
+#pragma unroll
+    for (int k = 1; k < 2 * T - 2; ++k) addc_cc(f[k + 1], b[k]);
+    addc_cc(f[2 * T - 1], 0u);
+    addc(f[2 * T], 0u);
+    add_cc(f[T], cc[0]);
+#pragma unroll
+    for (int c = 1; c < T; ++c) addc_cc(f[T + c], cc[c]);
+    addc(f[2 * T], cc[T]);
 }
 
 template <int T, int NT>
@@ -77,12 +101,14 @@ struct MulShape {
     static constexpr int BLOCK = NT > 256 ? NT : 256;
     static constexpr int IPB = BLOCK / NT;            // instances per block
     static constexpr int WPAD = NT * T;               // padded limbs per operand
-    static constexpr int ACC = 2 * T + 1;             // accumulator words
-    static constexpr int NCC = T + 1;                 // carry counters
-    static constexpr int SNAP = 4 * ((ACC + NCC + 3) / 4);
-    static constexpr int COMB = 4 * ((2 * ACC + 3) / 4);
+    static constexpr int ACC = 2 * T + 1;             // folded accumulator words
+    static constexpr int SNAP = 4 * ((DiagAcc<T>::WORDS + 3) / 4);
+    static constexpr int COMB = 2 * ACC;
     static constexpr int PER_T = COMB > SNAP ? COMB : SNAP;
-    static constexpr size_t SMEM = size_t(2 * IPB * WPAD + BLOCK * PER_T + BLOCK / 32) * 4;
+    // operands (2 x IPB x WPAD) + per-thread snapshot/combine slots; the
+    // carry resolution's per-warp words reuse the operand area.
+    static constexpr size_t SMEM = size_t(2 * IPB * WPAD + BLOCK * PER_T) * 4;
+    static_assert(PER_T % 4 == 0, "16-byte slots");
 };
 
 template <int T, int NT, bool VEC>
@@ -91,17 +117,19 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
           uint32_t n32, bool full) {
     using S = MulShape<T, NT>;
     constexpr int ACC = S::ACC;
-    constexpr int NCC = S::NCC;
+    static_assert(T == 8, "staging and plane layout assume 8-limb tiles");
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* sA = smem;
     uint32_t* sB = sA + S::IPB * S::WPAD;
     uint32_t* sT = sB + S::IPB * S::WPAD;
-    uint32_t* sScr = sT + S::BLOCK * S::PER_T;
+    uint32_t* sScr = sA;  // free once the tile loop is done
 
     const uint32_t grp = threadIdx.x / NT;
     const uint32_t t = threadIdx.x % NT;
     uint32_t* gA = sA + grp * S::WPAD;
-    uint32_t* gB = sB + grp * S::WPAD;
+    // B blocks in two planes of 16-byte halves: half q of block j is slot
+    // q*NT + j, so a group reading blocks (t-k) mod NT hits consecutive slots.
+    uint4* gB4 = reinterpret_cast<uint4*>(sB + grp * S::WPAD);
     uint32_t* mine = sT + threadIdx.x * S::PER_T;
     const uint32_t* gT = sT + grp * NT * S::PER_T;
     const uint32_t rlen = full ? 2 * n32 : n32;
@@ -116,7 +144,7 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
             const uint32_t* rb = b + (valid ? inst * n32 : 0);
 #pragma unroll
             for (int it = 0; it < T / 4; ++it) {
-                const uint32_t v = t + uint32_t(it) * NT;  // 16-byte slot
+                const uint32_t v = t + uint32_t(it) * NT;  // 16-byte slot of the operand
                 uint4 qa = make_uint4(0, 0, 0, 0), qb = qa;
                 if (VEC && valid && v * 4 + 4 <= n32) {
                     qa = __ldcs(reinterpret_cast<const uint4*>(ra) + v);
@@ -129,38 +157,43 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
                     if (w + 3 < n32) { qa.w = __ldcs(ra + w + 3); qb.w = __ldcs(rb + w + 3); }
                 }
                 reinterpret_cast<uint4*>(gA)[v] = qa;
-                reinterpret_cast<uint4*>(gB)[v] = qb;
+                gB4[(v & 1) * NT + (v >> 1)] = qb;
             }
         }
         __syncthreads();
 
         // 2. NT tiles per thread: A-block k times B-block (t-k) mod NT
-        uint32_t acc[ACC], cc[NCC];
+        DiagAcc<T> s;
 #pragma unroll
-        for (int w = 0; w < ACC; ++w) acc[w] = 0;
+        for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
 #pragma unroll
-        for (int w = 0; w < NCC; ++w) cc[w] = 0;
-#pragma unroll 1
+        for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
+#pragma unroll
+        for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+#pragma unroll 2
         for (uint32_t k = 0; k < uint32_t(NT); ++k) {
             const uint32_t j = (t - k) & uint32_t(NT - 1);
             uint32_t A[T], B[T];
-#pragma unroll
-            for (int q = 0; q < T / 4; ++q) {
-                const uint4 va = reinterpret_cast<const uint4*>(gA + k * T)[q];
-                const uint4 vb = reinterpret_cast<const uint4*>(gB + j * T)[q];
-                A[4 * q + 0] = va.x; A[4 * q + 1] = va.y; A[4 * q + 2] = va.z; A[4 * q + 3] = va.w;
-                B[4 * q + 0] = vb.x; B[4 * q + 1] = vb.y; B[4 * q + 2] = vb.z; B[4 * q + 3] = vb.w;
-            }
-            tile_mac<T>(A, B, acc, cc);
+            const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * T)[0];
+            const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * T)[1];
+            const uint4 b0 = gB4[j];
+            const uint4 b1 = gB4[NT + j];
+            A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
+            A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
+            B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
+            B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
+            tile_mac<T>(A, B, s);
             if (k == t) {
-                // anti-diagonal t is complete: snapshot accumulator + counters
+                // anti-diagonal t is complete: snapshot the accumulator
                 uint32_t tmp[S::SNAP];
 #pragma unroll
-                for (int w = 0; w < ACC; ++w) tmp[w] = acc[w];
+                for (int w = 0; w < 2 * T; ++w) tmp[w] = s.a[w];
 #pragma unroll
-                for (int w = 0; w < NCC; ++w) tmp[ACC + w] = cc[w];
+                for (int w = 0; w < 2 * T - 2; ++w) tmp[2 * T + w] = s.b[w];
 #pragma unroll
-                for (int w = ACC + NCC; w < S::SNAP; ++w) tmp[w] = 0;
+                for (int w = 0; w < T + 1; ++w) tmp[4 * T - 2 + w] = s.cc[w];
+#pragma unroll
+                for (int w = DiagAcc<T>::WORDS; w < S::SNAP; ++w) tmp[w] = 0;
 #pragma unroll
                 for (int q = 0; q < S::SNAP / 4; ++q)
                     reinterpret_cast<uint4*>(mine)[q] = make_uint4(tmp[4 * q], tmp[4 * q + 1], tmp[4 * q + 2], tmp[4 * q + 3]);
@@ -170,15 +203,14 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
         // 3. split into the two anti-diagonal values D1 (s=t) and D2 (s=t+NT)
         uint32_t d1[ACC], d2[ACC];
         {
-            fold_counters<T>(acc, cc);
-            uint32_t scc[NCC];
+            uint32_t snap[S::SNAP];
 #pragma unroll
-            for (int w = 0; w < ACC; ++w) d1[w] = mine[w];
-#pragma unroll
-            for (int w = 0; w < NCC; ++w) scc[w] = mine[ACC + w];
-            fold_counters<T>(d1, scc);
-#pragma unroll
-            for (int w = 0; w < ACC; ++w) d2[w] = acc[w];
+            for (int q = 0; q < S::SNAP / 4; ++q) {
+                const uint4 v = reinterpret_cast<const uint4*>(mine)[q];
+                snap[4 * q] = v.x; snap[4 * q + 1] = v.y; snap[4 * q + 2] = v.z; snap[4 * q + 3] = v.w;
+            }
+            fold<T>(snap, snap + 2 * T, snap + 4 * T - 2, d1);
+            fold<T>(s.a, s.b, s.cc, d2);
             sub_cc(d2[0], d1[0]);
 #pragma unroll
             for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
