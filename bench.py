@@ -402,6 +402,9 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
     }
     del da, db, dr
 
+    res["ragged_200k"] = ragged_vs_plain(args, ctx, dev, stream, world, rank)
+    res["serving"] = serving_sweep(args, ctx, rank)
+
     # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
     a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
     with torch.cuda.stream(stream):
@@ -416,6 +419,132 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
     del da, db, dr
     torch.cuda.empty_cache()
     return res
+
+
+def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
+    """Ragged batch of 200000 mixed ops: the persistent ragged kernels
+    (replayed CUDA graph) against the plain per-size-class launches with both
+    operands zero-padded to the class.  Both are timed device-resident with
+    CUDA events; the two outputs are compared limb for limb."""
+    import torch
+
+    import midint
+    import workloads
+    from plainform import PlainBatch
+
+    ops, pool, out_limbs = workloads.ragged_ops(seed=workloads.SEED_BASE + 3 + 1000 * rank)
+    n = ops.size
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        d_ops = torch.from_numpy(ops.view(np.uint8).copy()).to(dev)
+        d_in = torch.from_numpy(pool.view(np.int64)).to(dev)
+        d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+        d_c = torch.empty(n, dtype=torch.uint8, device=dev)
+        sb = midint.ragged_scratch_bytes(n)
+        scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    graph = ctx.ragged_graph(d_ops, n, d_in, d_out, scr, sb, carry=d_c)
+    steps = max(5, min(args.steps, 20))
+    ms_r = max_over_ranks(world, time_device(lambda i: graph.launch(sp), 1, steps, max(3, args.warmup), stream))
+    invalid = midint.ragged_invalid(scr)
+    out_r = d_out.cpu().numpy().view(np.uint64).copy()
+    carry_r = d_c.cpu().numpy().copy()
+    graph.close()
+
+    plain = PlainBatch(ops, pool, device=dev)
+    launches = [0]
+
+    def plain_step(i):
+        launches[0] = plain.run(ctx, sp)
+
+    ms_p = max_over_ranks(world, time_device(plain_step, 1, steps, max(3, args.warmup), stream))
+    out_p, carry_p = plain.results(ops, out_limbs)
+    adds = ops["kind"] == 0
+    same = bool(np.array_equal(out_r, out_p) and np.array_equal(carry_r[adds], carry_p[adds]))
+    la, lb = ops["la"].astype(np.int64), ops["lb"].astype(np.int64)
+    muls = ops["kind"] == 1
+    del plain, d_ops, d_in, d_out, d_c, scr
+    torch.cuda.empty_cache()
+    if not same:
+        raise SystemExit("bench: ragged and plain-form results differ")
+    return {
+        "config": "200000 ops, 40% add / 60% mul, operand bits log-uniform in [256, 65536] (4..1024 u64 limbs), "
+                  "independent lengths; adds return max(la,lb) limbs + carry, muls la+lb limbs",
+        "ragged_ms": ms_r, "ragged_ops/s": world * n / (ms_r * 1e-3),
+        "plain_ms": ms_p, "plain_ops/s": world * n / (ms_p * 1e-3), "plain_launches": launches[0],
+        "ragged_vs_plain": ms_p / ms_r,
+        "mul_partial_products": int((la[muls] * lb[muls]).sum() * 4),
+        "results_identical": same, "invalid_ops": invalid,
+        "ragged_path": "one CUDA graph: classify, scan, scatter, persistent NTT / classical / add kernels",
+    }
+
+
+def make_requests(count: int, seed: int):
+    """Serving requests: 1..512 ops each, operand bits log-uniform in
+    [512, 32768], 50/50 add/mul, seeded limbs."""
+    import workloads
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    lo, hi = np.log(512), np.log(32768)
+    for i in range(count):
+        n = int(rng.integers(1, 513))
+        kind = rng.integers(0, 2, n).astype(np.uint32)
+        la = np.ceil(np.exp(rng.uniform(lo, hi, n)) / 64).astype(np.uint32)
+        lb = np.ceil(np.exp(rng.uniform(lo, hi, n)) / 64).astype(np.uint32)
+        reqs.append(workloads.pack_ops(kind, la, lb, seed * 7919 + i))
+    return reqs
+
+
+def serve_once(ctx, reqs, rate: float | None, batching: bool, seed: int) -> dict:
+    """Submits every request (all at once if rate is None, else at Poisson
+    arrival times of that mean rate) and returns throughput and latency."""
+    import midint
+
+    outs = [np.zeros(r[2], np.uint64) for r in reqs]
+    carries = [np.zeros(r[0].size, np.uint8) for r in reqs]
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+    arrivals = np.cumsum(gaps)
+    with midint.Server(ctx, device_bytes=2 << 30, slots=3, batching=batching) as srv:
+        tickets = []
+        t0 = time.perf_counter()
+        for (ops, pool, _), out, c, at in zip(reqs, outs, carries, arrivals):
+            while time.perf_counter() - t0 < at:
+                pass
+            tickets.append(srv.submit(ops, pool, out, c))
+        for t in tickets:
+            srv.wait(t)
+        times = np.array([srv.times(t) for t in tickets], dtype=np.float64)
+        batches, _, n_ops = srv.stats()
+    lat = (times[:, 2] - times[:, 0]) * 1e-6
+    span = (times[:, 2].max() - times[:, 0].min()) * 1e-9
+    return {"offered_req/s": rate, "achieved_req/s": len(reqs) / span, "ops/s": n_ops / span,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "batches": batches, "requests": len(reqs)}
+
+
+def serving_sweep(args, ctx, rank) -> dict:
+    """Open-loop Poisson arrivals at fractions of the batched loop's capacity,
+    for continuous batching and for the plain per-request launch."""
+    reqs = make_requests(400, seed=workloads_seed(rank))
+    cap = serve_once(ctx, reqs, None, True, 1)          # closed loop: capacity
+    cap_plain = serve_once(ctx, reqs, None, False, 1)
+    out = {"config": "400 requests of U[1,512] ops (50/50 add/mul), operand bits log-uniform in [512, 32768]; "
+                     "open-loop Poisson arrivals; latency = submit -> results in the caller's host buffers",
+           "capacity_batched": cap, "capacity_per_request": cap_plain, "sweep": []}
+    for frac in (0.25, 0.5, 0.8):
+        rate = frac * cap["achieved_req/s"]
+        out["sweep"].append({"load_fraction_of_batched_capacity": frac,
+                             "batched": serve_once(ctx, reqs, rate, True, 2),
+                             "per_request": serve_once(ctx, reqs, rate, False, 2)})
+    return out
+
+
+def workloads_seed(rank: int) -> int:
+    import workloads
+
+    return workloads.SEED_BASE + 4 + 1000 * rank
 
 
 def run_reference(args):

@@ -77,6 +77,13 @@ mi_status mi_ctx_synchronize(mi_ctx ctx);
 /* The context's own stream, as a cudaStream_t. */
 mi_stream mi_ctx_stream(mi_ctx ctx);
 
+/* Classical/NTT crossovers of a context, in u64 limbs: ragged runs send a
+ * product through the NTT kernel when its shorter operand has at least
+ * ragged_ntt_min limbs (1..129; classical groups hold at most 128), and
+ * mi_mul_u64 does so when its operands have at least plain_ntt_min limbs
+ * (1..1025; 1025 = never).  Defaults come from the committed tuning table. */
+mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min);
+
 /* ---------------------------------------------------------------------------
  * Batched addition  r = (a + b) mod 2^(bits*limbs), carry_out[i] = carry bit.
  * Replaces baddKer<Base,IPB,M,Q> (cuda/ker-addition.cu.h:227-260) as launched
@@ -162,6 +169,95 @@ mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b,
                           uint64_t* h_r, uint8_t* h_carry, uint32_t n, uint32_t limbs);
 mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b,
                                uint64_t* h_r, uint32_t n, uint32_t limbs);
+
+/* ---------------------------------------------------------------------------
+ * Ragged batches: one list of adds and multiplies of uneven lengths, run by
+ * persistent kernels that bin the list by size class on the device.  No
+ * reference counterpart: the reference launches one kernel per operation and
+ * size (cuda/main.cu:661-746) with both operands of one compile-time size.
+ *
+ * Each op reads a (la limbs) and b (lb limbs) from the u64 input pool at limb
+ * offsets a_off, b_off and writes its result at limb offset r_off of the
+ * output pool: an add writes max(la, lb) limbs (the sum modulo 2^(64 max))
+ * and, if carry_out is given, carry_out[op index]; a multiply writes la + lb
+ * limbs (the full product).  1 <= la, lb <= 1024.  Results must not overlap
+ * each other or the inputs.  Ops with a bad kind or length are skipped and
+ * counted (mi_ragged_invalid).
+ * ------------------------------------------------------------------------- */
+#define MI_OP_ADD 0u
+#define MI_OP_MUL 1u
+
+typedef struct mi_op {
+    uint32_t kind;  /* MI_OP_ADD or MI_OP_MUL */
+    uint32_t la;    /* limbs of a */
+    uint32_t lb;    /* limbs of b */
+    uint32_t flags; /* reserved, 0 */
+    uint64_t a_off; /* limb offset of a in the input pool */
+    uint64_t b_off; /* limb offset of b in the input pool */
+    uint64_t r_off; /* limb offset of the result in the output pool */
+} mi_op;
+
+/* Device scratch a ragged run needs for n_ops operations. */
+mi_status mi_ragged_scratch_bytes(uint32_t n_ops, size_t* bytes);
+
+/* Runs the ops (device arrays) asynchronously on `stream`: classify, scan,
+ * scatter, then one persistent kernel per family (NTT products, classical
+ * rectangular products, additions), each consuming its tasks longest first
+ * from an atomic queue.  `scratch` is caller-owned device memory of at least
+ * mi_ragged_scratch_bytes(n_ops).  The first call on a device loads the
+ * size-class order tables; make it before capturing a stream. */
+mi_status mi_ragged_run(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                        uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_stream stream);
+
+/* Number of ops the last run on this scratch skipped as invalid (synchronous). */
+mi_status mi_ragged_invalid(const void* scratch, uint32_t* count);
+
+/* The same run captured once into a CUDA graph and replayed. */
+typedef struct mi_graph_s* mi_graph;
+mi_status mi_ragged_graph_create(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                                 uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_graph* graph);
+mi_status mi_graph_launch(mi_graph graph, mi_stream stream);
+mi_status mi_graph_destroy(mi_graph graph);
+
+/* ---------------------------------------------------------------------------
+ * Serving: a request loop with continuous batching.  No reference
+ * counterpart (the reference runs one synchronous batch per size).
+ *
+ * A request is a ragged op list (mi_op, offsets into the request's own pools)
+ * with host buffers that stay valid until it completes.  A loop thread
+ * admits queued requests FIFO into the next free batch slot while the slot's
+ * device arena has room (memory-based admission), so requests that arrive
+ * while other batches are on the GPU join the next batch; each slot has its
+ * own stream, so batches overlap on the device.  batching = 0 gives the plain
+ * per-request form: one request per launch, one slot.
+ * ------------------------------------------------------------------------- */
+typedef struct mi_server_s* mi_server;
+
+typedef struct mi_server_config {
+    size_t device_bytes;    /* device memory for in-flight batches (0 = 1/4 of free memory) */
+    uint32_t slots;         /* batches in flight at once, 1..8 */
+    uint32_t max_batch_ops; /* cap on ops per batch (0 = none) */
+    uint32_t batching;      /* 1 = continuous batching, 0 = one request per launch */
+    uint32_t reserved;      /* 0 */
+} mi_server_config;
+
+mi_status mi_server_create(mi_ctx ctx, const mi_server_config* config, mi_server* server);
+/* Finishes every queued and in-flight request, then frees the server. */
+mi_status mi_server_destroy(mi_server server);
+/* Queues a request; non-blocking.  Ops must stay inside the request's pools
+ * (in: in_limbs limbs, out: out_limbs limbs); carry_out may be NULL. */
+mi_status mi_server_submit(mi_server server, const mi_op* ops, uint32_t n_ops, const uint64_t* in,
+                           size_t in_limbs, uint64_t* out, size_t out_limbs, uint8_t* carry_out,
+                           uint64_t* ticket);
+/* Waits for a request (timeout_ms < 0: no limit); MI_ETIMEOUT if not done. */
+mi_status mi_server_wait(mi_server server, uint64_t ticket, int timeout_ms);
+/* Host steady-clock times (ns) of submission, admission and completion. */
+mi_status mi_server_request_times(mi_server server, uint64_t ticket, uint64_t* submit_ns,
+                                  uint64_t* admit_ns, uint64_t* done_ns);
+/* Forgets a finished request. */
+mi_status mi_server_release(mi_server server, uint64_t ticket);
+/* Batches launched, requests and ops finished so far. */
+mi_status mi_server_stats(mi_server server, uint64_t* batches, uint64_t* requests, uint64_t* ops);
 
 /* ---------------------------------------------------------------------------
  * Calibration: throughput of the integer multiply pipe on this device, in

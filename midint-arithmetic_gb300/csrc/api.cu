@@ -13,19 +13,9 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "ctx.h"
 #include "kernels.h"
 #include "ntt_host.h"
-
-struct mi_ctx_s {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    mi::NttTables ntt;  // resident twiddles of the three NTT primes
-    // host-pointer pipeline: two streams, each with its own device staging area
-    cudaStream_t pipe[2] = {nullptr, nullptr};
-    void* stage[2] = {nullptr, nullptr};
-    size_t stage_cap = 0;
-    std::mutex mu;  // serialises host-pointer calls on one context
-};
 
 namespace mi {
 
@@ -133,8 +123,6 @@ mi_status mul_ntt(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
     return launch_mul_ntt(a, b, r, n, limbs, ctx->ntt.params, pick_stream(ctx, stream));
 }
 
-// Size at and above which the full product goes through the NTT kernel.
-constexpr uint32_t kNttCrossoverLimbs = 256;
 
 // --- default contexts for the reference-shaped host-pointer wrappers -------
 std::mutex g_default_mu;
@@ -276,6 +264,17 @@ mi_status mi_ctx_synchronize(mi_ctx ctx) {
 
 mi_stream mi_ctx_stream(mi_ctx ctx) { return ctx ? reinterpret_cast<mi_stream>(ctx->stream) : nullptr; }
 
+mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min) {
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    if (ragged_ntt_min < 1 || ragged_ntt_min > 129)
+        return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..129", ragged_ntt_min);
+    if (plain_ntt_min < 1 || plain_ntt_min > kNttMaxLimbs + 1)
+        return set_error(MI_EINVAL, "plain_ntt_min %u outside 1..%u", plain_ntt_min, kNttMaxLimbs + 1);
+    ctx->ragged_ntt_min = ragged_ntt_min;
+    ctx->plain_ntt_min = plain_ntt_min;
+    return MI_OK;
+}
+
 mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry_out, uint32_t n,
                      uint32_t limbs, mi_stream stream) {
     return add_any(ctx, a, b, r, carry_out, n, limbs, stream, 8, ADD_PLAIN);
@@ -315,7 +314,8 @@ mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint6
 
 mi_status mi_mul_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                      mi_stream stream) {
-    if (limbs >= kNttCrossoverLimbs && limbs <= kNttMaxLimbs) return mul_ntt(ctx, a, b, r, n, limbs, stream);
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    if (limbs >= ctx->plain_ntt_min && limbs <= kNttMaxLimbs) return mul_ntt(ctx, a, b, r, n, limbs, stream);
     return mul_any(ctx, a, b, r, n, limbs, stream, 8, true);
 }
 
@@ -389,6 +389,81 @@ mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t*
                              return launch_mul_ntt(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
                                                    static_cast<uint64_t*>(dr), cnt, m, ctx->ntt.params, st, true);
                          });
+}
+
+// --- ragged batches ----------------------------------------------------------
+
+mi_status mi_ragged_scratch_bytes(uint32_t n_ops, size_t* bytes) {
+    if (bytes == nullptr) return set_error(MI_EINVAL, "ragged_scratch_bytes: null out");
+    *bytes = ragged_scratch_words(n_ops) * 4;
+    return MI_OK;
+}
+
+mi_status mi_ragged_run(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                        uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_stream stream) {
+    if (n_ops == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    return ragged_launch(ctx, ops, n_ops, in, out, carry_out, scratch, scratch_bytes, ctx->ragged_ntt_min,
+                         pick_stream(ctx, stream));
+}
+
+mi_status mi_ragged_invalid(const void* scratch, uint32_t* count) {
+    if (scratch == nullptr || count == nullptr) return set_error(MI_EINVAL, "ragged_invalid: null pointer");
+    MI_CUDA_TRY(cudaMemcpy(count, static_cast<const uint32_t*>(scratch) + ragged_invalid_word(), 4,
+                           cudaMemcpyDeviceToHost));
+    return MI_OK;
+}
+
+mi_status mi_ragged_graph_create(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                                 uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_graph* graph) {
+    if (graph == nullptr) return set_error(MI_EINVAL, "ragged_graph_create: null out");
+    *graph = nullptr;
+    MI_TRY(check_ctx(ctx));
+    MI_TRY(ragged_prepare());  // constant tables and attributes, outside the capture
+    cudaStream_t cs = nullptr;
+    MI_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    mi_graph g = new (std::nothrow) mi_graph_s();
+    if (g == nullptr) {
+        cudaStreamDestroy(cs);
+        return set_error(MI_ENOMEM, "ragged_graph_create: host allocation");
+    }
+    g->device = ctx->device;
+    mi_status st = MI_OK;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) st = cuda_error(e, "cudaStreamBeginCapture");
+    if (st == MI_OK) {
+        const mi_status launched =
+            ragged_launch(ctx, ops, n_ops, in, out, carry_out, scratch, scratch_bytes, ctx->ragged_ntt_min, cs);
+        e = cudaStreamEndCapture(cs, &g->graph);
+        if (launched != MI_OK) st = launched;
+        else if (e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture");
+    }
+    if (st == MI_OK && g->graph != nullptr) {
+        e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (e != cudaSuccess) st = cuda_error(e, "cudaGraphInstantiate");
+    }
+    cudaStreamDestroy(cs);
+    if (st != MI_OK) {
+        mi_graph_destroy(g);
+        return st;
+    }
+    *graph = g;
+    return MI_OK;
+}
+
+mi_status mi_graph_launch(mi_graph graph, mi_stream stream) {
+    if (graph == nullptr || graph->exec == nullptr) return set_error(MI_EINVAL, "graph_launch: null graph");
+    MI_CUDA_TRY(cudaSetDevice(graph->device));
+    MI_CUDA_TRY(cudaGraphLaunch(graph->exec, reinterpret_cast<cudaStream_t>(stream)));
+    return MI_OK;
+}
+
+mi_status mi_graph_destroy(mi_graph graph) {
+    if (graph == nullptr) return MI_OK;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    delete graph;
+    return MI_OK;
 }
 
 // --- host-buffer end-to-end calls -------------------------------------------

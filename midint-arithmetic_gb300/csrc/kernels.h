@@ -22,6 +22,15 @@ mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
                              bool full, cudaStream_t st);
 
+// Ragged batches (ragged.cu): device scratch words for n_ops, the word that
+// counts skipped ops, the one-time per-device setup (call outside stream
+// capture) and the asynchronous launch sequence.
+size_t ragged_scratch_words(uint32_t n_ops);
+size_t ragged_invalid_word();
+mi_status ragged_prepare();
+mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                        uint8_t* carry, void* scratch, size_t scratch_bytes, uint32_t ntt_min, cudaStream_t st);
+
 // Largest u32 limb count the classical kernel takes per instance.
 constexpr uint32_t kMulMaxN32 = 2048;
 // Largest u64 limb count the addition kernels take per instance (one group of

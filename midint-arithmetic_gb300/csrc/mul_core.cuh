@@ -1,0 +1,282 @@
+// mul_core.cuh -- the square-product building block of the classical
+// multiplication kernels (the plain batched kernel in mul.cu and the chunked
+// rectangular products of the ragged kernels in ragged.cu).
+//
+// Counterpart of the reference's bmulRegsQ and its helpers computeIter64 /
+// convolutionQ / combineQ / from4Reg2ShmQ (cuda/ker-classic-mul.cu.h:11-26,
+// 299-463).  The reference walks output columns with a 128-bit accumulator and
+// a carry counter, reading both operands from shared memory for every 64x64-bit
+// product, and balances the low-half triangle by pairing column k with M-k.
+//
+// Here the grid of 32x32-bit partial products of two operands of NT*T limbs is
+// cut into T x T tiles (T = 8).  Thread t of a group of NT threads owns the
+// anti-diagonals of tiles s = t and s = t + NT, which together hold exactly NT
+// tiles for every t (t+1 below the main anti-diagonal, NT-1-t above), so the
+// full product is balanced without mirroring.  At step k every thread
+// multiplies A-block k (the same address for the whole group: a broadcast) by
+// B-block (t-k) mod NT, stored as two planes of 16-byte halves so that the
+// group reads consecutive 16-byte slots (no bank conflicts).
+//
+// A tile is 2*T*T multiply-adds with the hardware carry flag.  Products with
+// i+j even and with i+j odd go to two accumulators split by column parity, so
+// every (lo, hi) word pair of a product lands on an even-aligned register pair
+// (mad.lo.cc + madc.hi.cc on the same operands then issue as one wide
+// multiply-add) and each tile row is two independent carry chains; the single
+// carry-out of each chain goes into a per-column counter (one addc).  The
+// first anti-diagonal is snapshotted to shared memory at the step where it
+// completes (one predicated store sequence per step); the second is the final
+// accumulator minus the snapshot.  Every output block of T limbs is then
+// L_s + H_(s-1) + O_(s-2) (low, high and overflow words of the anti-diagonal
+// values), added with two carry-lookahead passes over the group
+// (mi::group_carry) -- the reference's low/high/carry publish and baddRegs.
+#pragma once
+
+#include "common.cuh"
+
+namespace mi {
+namespace classic {
+
+constexpr int T = 8;  // tile side, in 32-bit limbs
+
+// Accumulator of one anti-diagonal, split by column parity:
+//   a[c]  column c,   products with i+j even (chains start at even columns)
+//   b[k]  column k+1, products with i+j odd
+//   cc[c] carries out of the chains, at column T+c
+struct DiagAcc {
+    uint32_t a[2 * T];
+    uint32_t b[2 * T - 2];
+    uint32_t cc[T + 1];
+    static constexpr int WORDS = 2 * T + 2 * T - 2 + T + 1;  // 39
+};
+
+constexpr int ACC = 2 * T + 1;                  // words of a folded anti-diagonal value
+constexpr int SNAP = 4 * ((DiagAcc::WORDS + 3) / 4);
+constexpr int PER_T = SNAP > 2 * ACC ? SNAP : 2 * ACC;  // shared words per thread (40)
+
+__device__ __forceinline__ void tile_mac(const uint32_t (&A)[T], const uint32_t (&B)[T], DiagAcc& s) {
+#pragma unroll
+    for (int i = 0; i < T; ++i) {
+        const int j0 = i & 1;  // first j with i+j even: columns i+j0 .. i+j0+T-1
+        mad_lo_cc(s.a[i + j0], A[i], B[j0]);
+        madc_hi_cc(s.a[i + j0 + 1], A[i], B[j0]);
+#pragma unroll
+        for (int j = j0 + 2; j < T; j += 2) {
+            madc_lo_cc(s.a[i + j], A[i], B[j]);
+            madc_hi_cc(s.a[i + j + 1], A[i], B[j]);
+        }
+        addc(s.cc[i + j0], 0u);
+        const int j1 = 1 - j0;  // first j with i+j odd: columns i+j1 .. i+j1+T-1
+        mad_lo_cc(s.b[i + j1 - 1], A[i], B[j1]);
+        madc_hi_cc(s.b[i + j1], A[i], B[j1]);
+#pragma unroll
+        for (int j = j1 + 2; j < T; j += 2) {
+            madc_lo_cc(s.b[i + j - 1], A[i], B[j]);
+            madc_hi_cc(s.b[i + j], A[i], B[j]);
+        }
+        addc(s.cc[i + j1], 0u);
+    }
+}
+
+// The (2T+1)-word value a + b*2^32 + cc*2^(32T) of an accumulator; the true
+// value of an anti-diagonal of at most 2^31 tiles always fits.
+__device__ __forceinline__ void fold(const uint32_t* a, const uint32_t* b, const uint32_t* cc, uint32_t (&f)[ACC]) {
+#pragma unroll
+    for (int c = 0; c < 2 * T; ++c) f[c] = a[c];
+    f[2 * T] = 0;
+    add_cc(f[1], b[0]);
+#pragma unroll
+    for (int k = 1; k < 2 * T - 2; ++k) addc_cc(f[k + 1], b[k]);
+    addc_cc(f[2 * T - 1], 0u);
+    addc(f[2 * T], 0u);
+    add_cc(f[T], cc[0]);
+#pragma unroll
+    for (int c = 1; c < T; ++c) addc_cc(f[T + c], cc[c]);
+    addc(f[2 * T], cc[T]);
+}
+
+// Stages `n32` limbs of an operand row into the group's A area (blocks of T
+// consecutive limbs), zero padded to NT*T limbs.  VEC: the row is 16-byte
+// aligned and n32 % 4 == 0.
+template <int NT, bool VEC>
+__device__ __forceinline__ void stage_a(uint32_t* gA, const uint32_t* __restrict__ row, uint32_t n32, bool valid,
+                                        uint32_t t) {
+#pragma unroll
+    for (int it = 0; it < T / 4; ++it) {
+        const uint32_t v = t + uint32_t(it) * NT;  // 16-byte slot of the operand
+        uint4 q = make_uint4(0, 0, 0, 0);
+        if (VEC && valid && v * 4 + 4 <= n32) {
+            q = __ldcs(reinterpret_cast<const uint4*>(row) + v);
+        } else if (valid) {
+            const uint32_t w = v * 4;
+            if (w + 0 < n32) q.x = __ldcs(row + w + 0);
+            if (w + 1 < n32) q.y = __ldcs(row + w + 1);
+            if (w + 2 < n32) q.z = __ldcs(row + w + 2);
+            if (w + 3 < n32) q.w = __ldcs(row + w + 3);
+        }
+        reinterpret_cast<uint4*>(gA)[v] = q;
+    }
+}
+
+// Same for the B operand, in the two-plane layout: half h of block j is 16-byte
+// slot h*NT + j.
+template <int NT, bool VEC>
+__device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__ row, uint32_t n32, bool valid,
+                                        uint32_t t) {
+#pragma unroll
+    for (int it = 0; it < T / 4; ++it) {
+        const uint32_t v = t + uint32_t(it) * NT;
+        uint4 q = make_uint4(0, 0, 0, 0);
+        if (VEC && valid && v * 4 + 4 <= n32) {
+            q = __ldcs(reinterpret_cast<const uint4*>(row) + v);
+        } else if (valid) {
+            const uint32_t w = v * 4;
+            if (w + 0 < n32) q.x = __ldcs(row + w + 0);
+            if (w + 1 < n32) q.y = __ldcs(row + w + 1);
+            if (w + 2 < n32) q.z = __ldcs(row + w + 2);
+            if (w + 3 < n32) q.w = __ldcs(row + w + 3);
+        }
+        gB4[(v & 1) * NT + (v >> 1)] = q;
+    }
+}
+
+// The full product of the group's staged A (NT blocks) and B (NT blocks).
+// On return thread t holds output blocks t (lo, limbs tT..tT+T-1) and t+NT
+// (hi), fully carried.  `mine` is the thread's PER_T shared words, `gT` the
+// group's first thread's, `scr` per-warp scratch for groups wider than a warp.
+// Starts and ends with the group's shared areas free for reuse by the caller
+// after a group_sync.
+template <int NT>
+__device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint32_t* mine, const uint32_t* gT,
+                                               uint32_t* scr, uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+    DiagAcc s;
+#pragma unroll
+    for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
+#pragma unroll
+    for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
+#pragma unroll
+    for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+#pragma unroll 2
+    for (uint32_t k = 0; k < uint32_t(NT); ++k) {
+        const uint32_t j = (t - k) & uint32_t(NT - 1);
+        uint32_t A[T], B[T];
+        const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * T)[0];
+        const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * T)[1];
+        const uint4 b0 = gB4[j];
+        const uint4 b1 = gB4[NT + j];
+        A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
+        A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
+        B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
+        B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
+        tile_mac(A, B, s);
+        if (k == t) {
+            // anti-diagonal t is complete: snapshot the accumulator
+            uint32_t tmp[SNAP];
+#pragma unroll
+            for (int w = 0; w < 2 * T; ++w) tmp[w] = s.a[w];
+#pragma unroll
+            for (int w = 0; w < 2 * T - 2; ++w) tmp[2 * T + w] = s.b[w];
+#pragma unroll
+            for (int w = 0; w < T + 1; ++w) tmp[4 * T - 2 + w] = s.cc[w];
+#pragma unroll
+            for (int w = DiagAcc::WORDS; w < SNAP; ++w) tmp[w] = 0;
+#pragma unroll
+            for (int q = 0; q < SNAP / 4; ++q)
+                reinterpret_cast<uint4*>(mine)[q] = make_uint4(tmp[4 * q], tmp[4 * q + 1], tmp[4 * q + 2], tmp[4 * q + 3]);
+        }
+    }
+
+    // split into the two anti-diagonal values D1 (s=t) and D2 (s=t+NT)
+    uint32_t d1[ACC], d2[ACC];
+    {
+        uint32_t snap[SNAP];
+#pragma unroll
+        for (int q = 0; q < SNAP / 4; ++q) {
+            const uint4 v = reinterpret_cast<const uint4*>(mine)[q];
+            snap[4 * q] = v.x; snap[4 * q + 1] = v.y; snap[4 * q + 2] = v.z; snap[4 * q + 3] = v.w;
+        }
+        fold(snap, snap + 2 * T, snap + 4 * T - 2, d1);
+        fold(s.a, s.b, s.cc, d2);
+        sub_cc(d2[0], d1[0]);
+#pragma unroll
+        for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
+        subc(d2[ACC - 1], d1[ACC - 1]);
+#pragma unroll
+        for (int w = 0; w < ACC; ++w) {
+            mine[w] = d1[w];
+            mine[ACC + w] = d2[w];
+        }
+    }
+    group_sync<NT>();
+
+    // output blocks s=t (lo) and s=t+NT (hi): L_s + H_(s-1) + O_(s-2)
+    auto peer = [&](uint32_t lane, int which, int w) -> uint32_t { return gT[lane * PER_T + which * ACC + w]; };
+    uint32_t Hlo[T], Hhi[T], Olo = 0, Ohi = 0;
+#pragma unroll
+    for (int w = 0; w < T; ++w) {
+        Hlo[w] = (t >= 1) ? peer(t - 1, 0, T + w) : 0u;
+        Hhi[w] = (t >= 1) ? peer(t - 1, 1, T + w) : peer(NT - 1, 0, T + w);
+    }
+    if (t >= 2) {
+        Olo = peer(t - 2, 0, 2 * T);
+        Ohi = peer(t - 2, 1, 2 * T);
+    } else {
+        if constexpr (NT >= 2) Ohi = (t == 1) ? peer(NT - 1, 0, 2 * T) : peer(NT - 2, 0, 2 * T);
+    }
+    uint32_t Llo[T], Lhi[T];
+#pragma unroll
+    for (int w = 0; w < T; ++w) {
+        Llo[w] = d1[w];
+        Lhi[w] = d2[w];
+    }
+    {
+        bool g0, p0, g1, p1;
+        uint32_t c0, c1;
+        chunk_add<uint32_t, T>(Llo, Hlo, ulo, g0, p0);
+        chunk_add<uint32_t, T>(Lhi, Hhi, uhi, g1, p1);
+        const uint32_t cl = group_carry<NT>(g0, p0, 0u, &c0, scr);
+        const uint32_t ch = group_carry<NT>(g1, p1, c0, &c1, scr);
+        chunk_inc<uint32_t, T>(ulo, cl);
+        chunk_inc<uint32_t, T>(uhi, ch);
+    }
+    {
+        uint32_t Zlo[T], Zhi[T];
+#pragma unroll
+        for (int w = 0; w < T; ++w) {
+            Zlo[w] = 0;
+            Zhi[w] = 0;
+        }
+        Zlo[0] = Olo;
+        Zhi[0] = Ohi;
+        uint32_t vlo[T], vhi[T];
+        bool g0, p0, g1, p1;
+        uint32_t c0, c1;
+        chunk_add<uint32_t, T>(ulo, Zlo, vlo, g0, p0);
+        chunk_add<uint32_t, T>(uhi, Zhi, vhi, g1, p1);
+        const uint32_t cl = group_carry<NT>(g0, p0, 0u, &c0, scr);
+        const uint32_t ch = group_carry<NT>(g1, p1, c0, &c1, scr);
+        chunk_inc<uint32_t, T>(vlo, cl);
+        chunk_inc<uint32_t, T>(vhi, ch);
+#pragma unroll
+        for (int w = 0; w < T; ++w) {
+            ulo[w] = vlo[w];
+            uhi[w] = vhi[w];
+        }
+    }
+}
+
+// Stores the T limbs of `v` at limb o of a result row, clipped to rlen.
+template <bool VEC>
+__device__ __forceinline__ void store_block(uint32_t* rr, uint32_t o, uint32_t rlen, const uint32_t (&v)[T]) {
+    if (VEC && o + T <= rlen) {
+#pragma unroll
+        for (int q = 0; q < T / 4; ++q)
+            __stcs(reinterpret_cast<uint4*>(rr + o) + q, make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+    } else {
+#pragma unroll
+        for (int w = 0; w < T; ++w)
+            if (o + w < rlen) __stcs(rr + o + w, v[w]);
+    }
+}
+
+}  // namespace classic
+}  // namespace mi

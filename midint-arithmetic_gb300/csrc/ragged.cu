@@ -1,0 +1,470 @@
+// ragged.cu -- one ragged list of additions and multiplications of uneven
+// lengths, binned by size class on the device and consumed by persistent
+// kernels, longest work first.  (No reference counterpart: the reference runs
+// one kernel per operation and compile-time size, cuda/main.cu:661-746.)
+//
+// Stages, all asynchronous on one stream (and so capturable in a CUDA graph):
+//  1. classify: each op gets a size-class key and bumps that key's count;
+//  2. scan (one block): op offsets per key and task offsets per family, with
+//     the keys of each family in descending cost order;
+//  3. scatter: op indices grouped by key;
+//  4. three persistent kernels, one per family, each popping tasks from its
+//     atomic queue:
+//     * NTT products (shorter operand >= the crossover): a task is one CTA of
+//       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh);
+//     * classical rectangular products: a task is one warp = 32/NT products
+//       whose shorter operand fits NT tiles of 8 u32 limbs; the longer one is
+//       consumed in chunks of NT tiles, each chunk a square product
+//       (mul_core.cuh) added into a sliding window whose low half is final --
+//       no padding of either operand to a power of two;
+//     * additions: a task is one CTA of groups sized to max(la, lb).
+// Within a family the key encodes everything that sets the trip counts of a
+// task, so the groups of a task run in lockstep.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "ctx.h"
+#include "kernels.h"
+#include "mul_core.cuh"
+#include "ntt_mul.cuh"
+
+namespace mi {
+namespace rg {
+
+constexpr uint32_t kMaxLimbs = 1024;
+constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11
+constexpr int K_CLS = 6 * 256;   // NT = 1..32 x chunks = 1..256
+constexpr int K_ADD = 10;        // (Q=2, GS=1..32), (Q=4, GS=32..256)
+constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = K_NTT + K_CLS;
+constexpr int K = KEY_ADD + K_ADD;
+constexpr uint32_t KEY_INVALID = 0xffffffffu;
+constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
+
+// Keys of each family in descending cost order (filled once per device).
+__constant__ uint16_t c_order[K];
+
+struct Scratch {  // word offsets into the scratch buffer
+    static constexpr size_t COUNTS = 0;
+    static constexpr size_t CURSORS = COUNTS + K;
+    static constexpr size_t OPOFF = CURSORS + K;
+    static constexpr size_t TS = OPOFF + K;             // task starts: K + 3 words (one extra per family)
+    static constexpr size_t NTASKS = TS + K + 3;        // 3 words
+    static constexpr size_t QUEUE = NTASKS + 3;         // 3 words
+    static constexpr size_t INVALID = QUEUE + 3;        // 1 word
+    static constexpr size_t KEYS = ((INVALID + 1 + 31) / 32) * 32;
+    __host__ __device__ static constexpr size_t sorted(uint32_t n) { return KEYS + n; }  // op indices by key
+    __host__ __device__ static constexpr size_t words(uint32_t n) { return KEYS + 2 * size_t(n); }
+};
+
+struct Params {
+    const mi_op* ops;
+    uint32_t n_ops;
+    const uint64_t* in;
+    uint64_t* out;
+    uint8_t* carry;
+    uint32_t* scr;  // scratch words
+    uint32_t ntt_min;
+    NttMulParams ntt;
+};
+
+__device__ __forceinline__ uint32_t ceil_log2(uint32_t x) { return x <= 1 ? 0 : 32 - __clz(x - 1); }
+
+__device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) {
+    const uint32_t la = op.la, lb = op.lb;
+    if (la == 0 || lb == 0 || la > kMaxLimbs || lb > kMaxLimbs) return KEY_INVALID;
+    if (op.kind == MI_OP_ADD) {
+        const uint32_t m = max(la, lb);
+        if (m <= 64) return KEY_ADD + ceil_log2((m + 1) / 2);
+        return KEY_ADD + 6 + ceil_log2((m + 3) / 4) - 5;
+    }
+    if (op.kind == MI_OP_MUL) {
+        const uint32_t s = min(la, lb), l = max(la, lb);
+        if (s >= ntt_min) {
+            // L must hold all la+lb output limbs (the top limb is the carry out
+            // of the last of the la+lb-1 coefficients), not only the coefficients
+            const uint32_t lg = max(8u, ceil_log2(la + lb));
+            return KEY_NTT + (lg - 8);
+        }
+        const uint32_t ntl = ceil_log2((2 * s + 7) / 8);  // NT = 2^ntl <= 32
+        const uint32_t nt = 1u << ntl;
+        const uint32_t chunks = (2 * l + 8 * nt - 1) / (8 * nt);
+        return KEY_CLS + ntl * 256 + (chunks - 1);
+    }
+    return KEY_INVALID;
+}
+
+__host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
+    if (key < KEY_CLS) return 2048u >> (8 + key);                    // NTT: 256 threads / (L/8)
+    if (key < KEY_ADD) return 32u >> ((key - KEY_CLS) / 256);        // classical: one warp
+    const uint32_t k = key - KEY_ADD;                                 // add: 256 threads / GS
+    const uint32_t gs = k < 6 ? (1u << k) : (32u << (k - 6));
+    return 256u / gs;
+}
+
+__global__ void k_classify(const mi_op* __restrict__ ops, uint32_t n, uint32_t* __restrict__ scr, uint32_t ntt_min) {
+    uint32_t* counts = scr + Scratch::COUNTS;
+    uint32_t* keys = scr + Scratch::KEYS;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = classify(ops[i], ntt_min);
+        keys[i] = key;
+        if (key == KEY_INVALID)
+            atomicAdd(scr + Scratch::INVALID, 1u);
+        else
+            atomicAdd(counts + key, 1u);
+    }
+}
+
+// One block of 1024 threads: exclusive scans over the keys in c_order.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ scr) {
+    constexpr int N = 2048;
+    __shared__ uint32_t s_ops[N], s_tasks[N];
+    const uint32_t* counts = scr + Scratch::COUNTS;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        uint32_t c = 0, tk = 0;
+        if (i < K) {
+            const uint32_t key = c_order[i];
+            c = counts[key];
+            const uint32_t opt = ops_per_task(key);
+            tk = (c + opt - 1) / opt;
+        }
+        s_ops[i] = c;
+        s_tasks[i] = tk;
+        if (i < K) scr[Scratch::CURSORS + i] = 0;
+    }
+    __syncthreads();
+    // inclusive Hillis-Steele scans of both arrays
+    for (int d = 1; d < N; d <<= 1) {
+        uint32_t v0[2], v1[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = threadIdx.x + h * 1024;
+            v0[h] = s_ops[i] + (i >= d ? s_ops[i - d] : 0);
+            v1[h] = s_tasks[i] + (i >= d ? s_tasks[i - d] : 0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = threadIdx.x + h * 1024;
+            s_ops[i] = v0[h];
+            s_tasks[i] = v1[h];
+        }
+        __syncthreads();
+    }
+    // op offsets (exclusive, global over the ordered keys) and per-family task starts
+    const int fam_start[4] = {KEY_NTT, KEY_CLS, KEY_ADD, K};
+    for (int i = threadIdx.x; i < K; i += blockDim.x) {
+        const uint32_t key = c_order[i];
+        scr[Scratch::OPOFF + key] = i ? s_ops[i - 1] : 0;
+        const int f = i < KEY_CLS ? 0 : (i < KEY_ADD ? 1 : 2);
+        const int base = fam_start[f];
+        const uint32_t before = base ? s_tasks[base - 1] : 0;
+        scr[Scratch::TS + f + i] = (i ? s_tasks[i - 1] : 0) - before;
+    }
+    if (threadIdx.x < 3) {
+        const int f = threadIdx.x;
+        const int base = fam_start[f], end = fam_start[f + 1];
+        const uint32_t before = base ? s_tasks[base - 1] : 0;
+        const uint32_t total = s_tasks[end - 1] - before;
+        scr[Scratch::TS + f + end] = total;  // sentinel
+        scr[Scratch::NTASKS + f] = total;
+        scr[Scratch::QUEUE + f] = 0;
+    }
+}
+
+__global__ void k_scatter(uint32_t n, uint32_t* __restrict__ scr) {
+    const uint32_t* keys = scr + Scratch::KEYS;
+    uint32_t* sorted = scr + Scratch::sorted(n);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        if (key == KEY_INVALID) continue;
+        const uint32_t pos = scr[Scratch::OPOFF + key] + atomicAdd(scr + Scratch::CURSORS + key, 1u);
+        sorted[pos] = i;
+    }
+}
+
+// Task t of family f -> (key, index of its first op in `sorted`, op count).
+struct Task {
+    uint32_t key, first, count;
+};
+
+__device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
+    const int base = f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : KEY_ADD);
+    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS : K_ADD);
+    const uint32_t* ts = scr + Scratch::TS + f + base;  // nk + 1 monotone starts
+    int lo = 0, hi = nk;                                // ts[lo] <= t < ts[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ts[mid] <= t) lo = mid; else hi = mid;
+    }
+    const uint32_t key = c_order[base + lo];
+    const uint32_t opt = ops_per_task(key);
+    const uint32_t local = t - ts[lo];
+    const uint32_t cnt = scr[Scratch::COUNTS + key];
+    Task T;
+    T.key = key;
+    T.first = scr[Scratch::OPOFF + key] + local * opt;
+    T.count = min(opt, cnt - local * opt);
+    return T;
+}
+
+// --- NTT family ----------------------------------------------------------------
+
+template <int LG>
+__device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint64_t* sm, uint32_t* scr_warp) {
+    constexpr int NT = (1 << LG) / 8;
+    const uint32_t g = threadIdx.x / NT;
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    uint64_t* gsm = sm + g * ntt::MulSmem<LG>::WORDS64;
+    if (g < tk.count) {
+        const mi_op op = P.ops[sorted[tk.first + g]];
+        ntt::mul_one<LG>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb, P.ntt, gsm,
+                         scr_warp);
+    } else {  // idle group: zero operands, no store, same barriers
+        ntt::mul_one<LG>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    uint32_t* scr_warp = reinterpret_cast<uint32_t*>(smem + 8192);  // after 64 KiB
+    __shared__ uint32_t s_task;
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 0];
+    for (;;) {
+        if (threadIdx.x == 0) s_task = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
+        __syncthreads();
+        const uint32_t t = s_task;
+        __syncthreads();
+        if (t >= ntasks) break;
+        const Task tk = decode(P.scr, 0, t);
+        switch (tk.key - KEY_NTT) {
+            case 0: ntt_task<8>(P, tk, smem, scr_warp); break;
+            case 1: ntt_task<9>(P, tk, smem, scr_warp); break;
+            case 2: ntt_task<10>(P, tk, smem, scr_warp); break;
+            default: ntt_task<11>(P, tk, smem, scr_warp); break;
+        }
+    }
+}
+
+// --- classical family ----------------------------------------------------------
+
+template <int NT>
+__device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* wsm) {
+    using classic::T;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t g = lane / NT, t = lane % NT;
+    if (g >= tk.count) return;  // groups synchronise only among their own lanes
+    const uint32_t chunks = (tk.key - KEY_CLS) % 256 + 1;
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    const mi_op op = P.ops[sorted[tk.first + g]];
+    uint32_t* gA = wsm + g * NT * T;
+    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g * 2 * NT;
+    uint32_t* slots = wsm + 512;
+    uint32_t* mine = slots + lane * classic::PER_T;
+    const uint32_t* gT = slots + g * NT * classic::PER_T;
+    // longer operand x is consumed in chunks of W limbs against the staged shorter y
+    const bool a_long = op.la >= op.lb;
+    const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
+    const uint32_t* y = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.b_off : op.a_off));
+    const uint32_t nx = 2 * (a_long ? op.la : op.lb), ny = 2 * (a_long ? op.lb : op.la);
+    uint32_t* rr = reinterpret_cast<uint32_t*>(P.out + op.r_off);
+    const uint32_t rlen = 2 * (op.la + op.lb);
+    constexpr uint32_t W = NT * T;
+    classic::stage_b<NT, false>(gB4, y, ny, true, t);
+    uint32_t pend[T];
+#pragma unroll
+    for (int w = 0; w < T; ++w) pend[w] = 0;
+    for (uint32_t c = 0; c < chunks; ++c) {
+        const uint32_t left = nx - c * W;
+        classic::stage_a<NT, false>(gA, x + c * W, left < W ? left : W, true, t);
+        group_sync<NT>();
+        uint32_t ulo[T], uhi[T];
+        classic::square_product<NT>(gA, gB4, mine, gT, nullptr, t, ulo, uhi);
+        // limbs [cW, (c+1)W) are final: the low half plus the pending window
+        uint32_t fin[T];
+        bool g0, p0;
+        uint32_t gc;
+        chunk_add<uint32_t, T>(ulo, pend, fin, g0, p0);
+        const uint32_t cin = group_carry<NT>(g0, p0, 0u, &gc, nullptr);
+        chunk_inc<uint32_t, T>(fin, cin);
+        classic::store_block<false>(rr, c * W + t * T, rlen, fin);
+        // the high half plus that carry becomes the next window (cannot overflow)
+        uint32_t z[T];
+#pragma unroll
+        for (int w = 0; w < T; ++w) z[w] = 0;
+        z[0] = (t == 0) ? gc : 0u;
+        bool g1, p1;
+        uint32_t gc1;
+        chunk_add<uint32_t, T>(uhi, z, pend, g1, p1);
+        const uint32_t cin1 = group_carry<NT>(g1, p1, 0u, &gc1, nullptr);
+        chunk_inc<uint32_t, T>(pend, cin1);
+        group_sync<NT>();  // gA and the slots are reused by the next chunk
+    }
+    classic::store_block<false>(rr, chunks * W + t * T, rlen, pend);
+}
+
+__global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
+    extern __shared__ __align__(16) uint32_t smem32[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    uint32_t* wsm = smem32 + warp * CLS_WARP_WORDS;
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 1];
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
+        t = __shfl_sync(MI_FULL_MASK, t, 0);
+        if (t >= ntasks) break;
+        const Task tk = decode(P.scr, 1, t);
+        switch ((tk.key - KEY_CLS) / 256) {
+            case 0: classic_task<1>(P, tk, wsm); break;
+            case 1: classic_task<2>(P, tk, wsm); break;
+            case 2: classic_task<4>(P, tk, wsm); break;
+            case 3: classic_task<8>(P, tk, wsm); break;
+            case 4: classic_task<16>(P, tk, wsm); break;
+            default: classic_task<32>(P, tk, wsm); break;
+        }
+        __syncwarp();
+    }
+}
+
+// --- addition family -------------------------------------------------------------
+
+template <int Q, int GS>
+__device__ __forceinline__ void add_task(const Params& P, const Task& tk, uint32_t* scr_warp) {
+    const uint32_t g = threadIdx.x / GS, t = threadIdx.x % GS;
+    const bool valid = g < tk.count;
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    const uint32_t idx = valid ? sorted[tk.first + g] : 0;
+    const mi_op op = valid ? P.ops[idx] : mi_op{};
+    const uint32_t m = max(op.la, op.lb);
+    const uint64_t* ar = P.in + op.a_off;
+    const uint64_t* br = P.in + op.b_off;
+    const uint32_t start = t * Q;
+    uint64_t x[Q], y[Q], s[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        x[q] = (valid && start + q < op.la) ? __ldcs(reinterpret_cast<const unsigned long long*>(ar + start + q)) : 0;
+        y[q] = (valid && start + q < op.lb) ? __ldcs(reinterpret_cast<const unsigned long long*>(br + start + q)) : 0;
+    }
+    bool gg, pp;
+    chunk_add<uint64_t, Q>(x, y, s, gg, pp);
+    uint32_t gc;
+    const uint32_t cin = group_carry<GS>(gg, pp, 0u, &gc, scr_warp);
+    chunk_inc<uint64_t, Q>(s, cin);
+    if (!valid) return;
+    uint64_t* rr = P.out + op.r_off;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+        if (start + q < m) rr[start + q] = s[q];
+    if (P.carry != nullptr) {
+        if (m < uint32_t(GS * Q)) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (start + q == m) P.carry[idx] = uint8_t(s[q]);
+        } else if (t == GS - 1) {
+            P.carry[idx] = uint8_t(gc);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
+    __shared__ uint32_t scr_warp[8];
+    __shared__ uint32_t s_task;
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 2];
+    for (;;) {
+        if (threadIdx.x == 0) s_task = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
+        __syncthreads();
+        const uint32_t t = s_task;
+        __syncthreads();
+        if (t >= ntasks) break;
+        const Task tk = decode(P.scr, 2, t);
+        switch (tk.key - KEY_ADD) {
+            case 0: add_task<2, 1>(P, tk, scr_warp); break;
+            case 1: add_task<2, 2>(P, tk, scr_warp); break;
+            case 2: add_task<2, 4>(P, tk, scr_warp); break;
+            case 3: add_task<2, 8>(P, tk, scr_warp); break;
+            case 4: add_task<2, 16>(P, tk, scr_warp); break;
+            case 5: add_task<2, 32>(P, tk, scr_warp); break;
+            case 6: add_task<4, 32>(P, tk, scr_warp); break;
+            case 7: add_task<4, 64>(P, tk, scr_warp); break;
+            case 8: add_task<4, 128>(P, tk, scr_warp); break;
+            default: add_task<4, 256>(P, tk, scr_warp); break;
+        }
+    }
+}
+
+// --- host side -------------------------------------------------------------------
+
+constexpr size_t kNttSmem = 65536 + 64;
+constexpr size_t kClsSmem = size_t(8) * CLS_WARP_WORDS * 4;
+
+std::mutex g_init_mu;
+bool g_init[64] = {};
+
+mi_status init_device() {
+    int dev = 0;
+    MI_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(MI_ENODEV, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g_init[dev]) return MI_OK;
+    // keys of each family in descending cost
+    std::vector<uint16_t> order(K);
+    for (int k = 0; k < K_NTT; ++k) order[KEY_NTT + k] = uint16_t(KEY_NTT + (K_NTT - 1 - k));
+    std::vector<int> cls(K_CLS);
+    for (int k = 0; k < K_CLS; ++k) cls[k] = k;
+    auto cost = [](int k) { return (1 << (k / 256)) * (k % 256 + 1); };  // NT x chunks
+    std::stable_sort(cls.begin(), cls.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
+    for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
+    MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_classic, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kClsSmem)));
+    g_init[dev] = true;
+    return MI_OK;
+}
+
+int persistent_grid(const void* kern, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return sm_count() * per_sm;
+}
+
+}  // namespace rg
+
+mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                        uint8_t* carry, void* scratch, size_t scratch_bytes, uint32_t ntt_min, cudaStream_t st) {
+    using namespace rg;
+    if (n_ops == 0) return MI_OK;
+    if (ops == nullptr || in == nullptr || out == nullptr || scratch == nullptr)
+        return set_error(MI_EINVAL, "ragged: null pointer");
+    if (scratch_bytes < Scratch::words(n_ops) * 4) return set_error(MI_EINVAL, "ragged: scratch too small");
+    MI_TRY(init_device());
+    Params P;
+    P.ops = ops;
+    P.n_ops = n_ops;
+    P.in = in;
+    P.out = out;
+    P.carry = carry;
+    P.scr = static_cast<uint32_t*>(scratch);
+    // classical groups hold at most 32 tiles (128 u64 limbs) of the shorter operand
+    P.ntt_min = ntt_min < 1 ? 1 : (ntt_min > 129 ? 129 : ntt_min);
+    P.ntt = ctx->ntt.params;
+    MI_CUDA_TRY(cudaMemsetAsync(P.scr, 0, (Scratch::KEYS) * 4, st));
+    const uint32_t blocks = std::min<uint32_t>((n_ops + 255) / 256, uint32_t(sm_count() * 8));
+    k_classify<<<blocks, 256, 0, st>>>(ops, n_ops, P.scr, P.ntt_min);
+    k_scan<<<1, 1024, 0, st>>>(P.scr);
+    k_scatter<<<blocks, 256, 0, st>>>(n_ops, P.scr);
+    k_rg_ntt<<<persistent_grid((const void*)k_rg_ntt, kNttSmem), 256, kNttSmem, st>>>(P);
+    k_rg_classic<<<persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st>>>(P);
+    k_rg_add<<<persistent_grid((const void*)k_rg_add, 0), 256, 0, st>>>(P);
+    MI_CUDA_TRY(cudaGetLastError());
+    return MI_OK;
+}
+
+size_t ragged_scratch_words(uint32_t n_ops) { return rg::Scratch::words(n_ops); }
+mi_status ragged_prepare() { return rg::init_device(); }
+size_t ragged_invalid_word() { return rg::Scratch::INVALID; }
+
+}  // namespace mi

@@ -40,6 +40,7 @@ SIGNATURES = {
     "mi_ctx_destroy": (_S, [_P]),
     "mi_ctx_synchronize": (_S, [_P]),
     "mi_ctx_stream": (_P, [_P]),
+    "mi_ctx_set_crossover": (_S, [_P, _U32, _U32]),
     "mi_add_u64": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add_u32": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add6_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
@@ -58,7 +59,34 @@ SIGNATURES = {
     "mi_mul_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_compat_gpuMulFFT_u16": (_S, [_I, _U32, _P, _P, _P]),
     "mi_ntt_raw": (_S, [ctypes.c_uint64, ctypes.c_uint64, _U32, _U32, _I, _P, _P, _P]),
+    "mi_ragged_scratch_bytes": (_S, [_U32, ctypes.POINTER(ctypes.c_size_t)]),
+    "mi_ragged_run": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "mi_ragged_invalid": (_S, [_P, ctypes.POINTER(_U32)]),
+    "mi_ragged_graph_create": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "mi_graph_launch": (_S, [_P, _P]),
+    "mi_graph_destroy": (_S, [_P]),
+    "mi_server_create": (_S, [_P, _P, ctypes.POINTER(_P)]),
+    "mi_server_destroy": (_S, [_P]),
+    "mi_server_submit": (_S, [_P, _P, _U32, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P,
+                              ctypes.POINTER(ctypes.c_uint64)]),
+    "mi_server_wait": (_S, [_P, ctypes.c_uint64, _I]),
+    "mi_server_request_times": (_S, [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+    "mi_server_release": (_S, [_P, ctypes.c_uint64]),
+    "mi_server_stats": (_S, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(ctypes.c_uint64)]),
 }
+
+
+class ServerConfig(ctypes.Structure):
+    """struct mi_server_config of include/midint.h."""
+    _fields_ = [("device_bytes", ctypes.c_size_t), ("slots", ctypes.c_uint32), ("max_batch_ops", ctypes.c_uint32),
+                ("batching", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+MI_OP_ADD, MI_OP_MUL = 0, 1
+# struct mi_op of include/midint.h (40 bytes)
+OP_DTYPE = np.dtype([("kind", "<u4"), ("la", "<u4"), ("lb", "<u4"), ("flags", "<u4"),
+                     ("a_off", "<u8"), ("b_off", "<u8"), ("r_off", "<u8")])
 
 
 class MidintError(RuntimeError):
@@ -124,6 +152,9 @@ class Context:
     def synchronize(self) -> None:
         check(load().mi_ctx_synchronize(self.handle))
 
+    def set_crossover(self, ragged_ntt_min: int, plain_ntt_min: int) -> None:
+        check(load().mi_ctx_set_crossover(self.handle, ragged_ntt_min, plain_ntt_min))
+
     def close(self) -> None:
         if self.handle:
             load().mi_ctx_destroy(self.handle)
@@ -165,6 +196,19 @@ class Context:
         """Full product, classical or NTT by size (u64 limbs)."""
         check(load().mi_mul_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
 
+    # --- ragged batches ------------------------------------------------------
+    def ragged_run(self, ops, n_ops: int, pool_in, pool_out, scratch, scratch_bytes: int, carry=None,
+                   stream=None) -> None:
+        """Runs a ragged list of mi_op records (device array) on the device."""
+        check(load().mi_ragged_run(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out), _ptr(carry),
+                                   _ptr(scratch), scratch_bytes, _ptr(stream)))
+
+    def ragged_graph(self, ops, n_ops: int, pool_in, pool_out, scratch, scratch_bytes: int, carry=None) -> "Graph":
+        h = ctypes.c_void_p()
+        check(load().mi_ragged_graph_create(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out),
+                                            _ptr(carry), _ptr(scratch), scratch_bytes, ctypes.byref(h)))
+        return Graph(h.value)
+
     # --- host-buffer end-to-end calls --------------------------------------
     def host_add(self, h_a: np.ndarray, h_b: np.ndarray, h_r: np.ndarray, h_carry: np.ndarray | None,
                  n: int, limbs: int) -> None:
@@ -172,6 +216,89 @@ class Context:
 
     def host_mul_full(self, h_a: np.ndarray, h_b: np.ndarray, h_r: np.ndarray, n: int, limbs: int) -> None:
         check(load().mi_host_mul_full_u64(self.handle, _ptr(h_a), _ptr(h_b), _ptr(h_r), n, limbs))
+
+
+class Graph:
+    """A captured ragged run (mi_graph)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def launch(self, stream=None) -> None:
+        check(load().mi_graph_launch(self.handle, _ptr(stream)))
+
+    def close(self) -> None:
+        if self.handle:
+            load().mi_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A request loop (mi_server) on a context: continuous batching, or one
+    request per launch with batching=False."""
+
+    def __init__(self, ctx: "Context", device_bytes: int = 1 << 30, slots: int = 3, max_batch_ops: int = 0,
+                 batching: bool = True):
+        cfg = ServerConfig(device_bytes, slots, max_batch_ops, 1 if batching else 0, 0)
+        h = ctypes.c_void_p()
+        check(load().mi_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h.value
+        self._keep = {}
+
+    def submit(self, ops: np.ndarray, pool_in: np.ndarray, out: np.ndarray, carry: np.ndarray | None = None) -> int:
+        """Queues a request (host arrays, kept alive until released)."""
+        t = ctypes.c_uint64()
+        check(load().mi_server_submit(self.handle, _ptr(ops), ops.size, _ptr(pool_in), pool_in.size, _ptr(out),
+                                      out.size, _ptr(carry), ctypes.byref(t)))
+        self._keep[t.value] = (ops, pool_in, out, carry)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> None:
+        check(load().mi_server_wait(self.handle, ticket, timeout_ms))
+
+    def times(self, ticket: int):
+        s, a, d = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(load().mi_server_request_times(self.handle, ticket, ctypes.byref(s), ctypes.byref(a), ctypes.byref(d)))
+        return s.value, a.value, d.value
+
+    def release(self, ticket: int) -> None:
+        check(load().mi_server_release(self.handle, ticket))
+        self._keep.pop(ticket, None)
+
+    def stats(self):
+        b, r, o = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(load().mi_server_stats(self.handle, ctypes.byref(b), ctypes.byref(r), ctypes.byref(o)))
+        return b.value, r.value, o.value
+
+    def close(self) -> None:
+        if self.handle:
+            load().mi_server_destroy(self.handle)
+            self.handle = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def ragged_scratch_bytes(n_ops: int) -> int:
+    v = ctypes.c_size_t()
+    check(load().mi_ragged_scratch_bytes(n_ops, ctypes.byref(v)))
+    return v.value
+
+
+def ragged_invalid(scratch) -> int:
+    v = ctypes.c_uint32()
+    check(load().mi_ragged_invalid(_ptr(scratch), ctypes.byref(v)))
+    return v.value
 
 
 def calib_mul32_peak(iters: int = 0) -> float:

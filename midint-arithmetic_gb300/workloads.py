@@ -8,7 +8,10 @@ here and on any other machine, sees the same integers.  Workloads:
 * classical multiplication: 16384 pairs of 8192-bit integers (128 u64 limbs ->
   256-limb product), uniform; the u32 variant is the same bytes as 256 u32 limbs;
 * NTT multiplication: 1024 pairs of 65536-bit integers (1024 u64 limbs),
-  uniform, with every 16th pair all ones (maximal coefficients).
+  uniform, with every 16th pair all ones (maximal coefficients);
+* ragged batch: 200000 operations, 40 % additions / 60 % multiplications,
+  each operand's bit length drawn independently log-uniform in [256, 65536]
+  and rounded up to whole u64 limbs (4 ... 1024 limbs), uniform limbs.
 
 The reference's own generator (ourMkRandom, cuda/helper.h:99-114) builds
 words from glibc rand() and never sets the low bit, so it almost never
@@ -64,3 +67,35 @@ def ntt_pairs(n: int = 1024, m: int = 1024, seed: int = SEED_BASE + 2, ones_ever
         a.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
         b.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
     return a, b
+
+
+def ragged_ops(n_ops: int = 200000, seed: int = SEED_BASE + 3, add_frac: float = 0.4,
+               min_bits: int = 256, max_bits: int = 65536):
+    """Ragged workload: (ops, pool_in, out_limbs).
+
+    ops: structured array of mi_op records (midint.OP_DTYPE layout); operands
+    packed a0 b0 a1 b1 ... in pool_in (u64); results packed in op order in an
+    output pool of out_limbs limbs (max(la, lb) per add, la + lb per mul)."""
+    rng = np.random.default_rng(seed)
+    kind = (rng.random(n_ops) >= add_frac).astype(np.uint32)  # 0 add, 1 mul
+    lo, hi = np.log(min_bits), np.log(max_bits)
+    la = np.ceil(np.exp(rng.uniform(lo, hi, n_ops)) / 64).astype(np.uint32)
+    lb = np.ceil(np.exp(rng.uniform(lo, hi, n_ops)) / 64).astype(np.uint32)
+    return pack_ops(kind, la, lb, seed)
+
+
+def pack_ops(kind: np.ndarray, la: np.ndarray, lb: np.ndarray, seed: int):
+    """mi_op records for the given kinds and lengths, with seeded operands."""
+    n = kind.size
+    dt = np.dtype([("kind", "<u4"), ("la", "<u4"), ("lb", "<u4"), ("flags", "<u4"),
+                   ("a_off", "<u8"), ("b_off", "<u8"), ("r_off", "<u8")])
+    ops = np.zeros(n, dt)
+    ops["kind"], ops["la"], ops["lb"] = kind, la, lb
+    pair = la.astype(np.uint64) + lb.astype(np.uint64)
+    starts = np.concatenate([[0], np.cumsum(pair)[:-1]]).astype(np.uint64)
+    ops["a_off"] = starts
+    ops["b_off"] = starts + la.astype(np.uint64)
+    rlen = np.where(kind == 0, np.maximum(la, lb), la + lb).astype(np.uint64)
+    ops["r_off"] = np.concatenate([[0], np.cumsum(rlen)[:-1]]).astype(np.uint64)
+    pool = splitmix64(seed ^ 0x7A99ED, int(pair.sum()))
+    return ops, pool, int(rlen.sum())
