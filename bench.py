@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
+    ap.add_argument("--ragged-ops", type=int, default=200000, help="ops in the ragged batch")
+    ap.add_argument("--sections", default="add,ntt,ragged,serving,u32",
+                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32)")
     return ap.parse_args()
 
 
@@ -333,17 +336,30 @@ def run_ours(args):
 
 
 def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
-    """Addition (GB/s, %HBM), NTT multiplication and the u32-limb variant."""
+    """Addition (GB/s, %HBM), NTT multiplication, ragged vs plain, serving and
+    the u32-limb variant, each selectable with --sections."""
+    res = {}
+    sections = set(args.sections.split(","))
+    if "add" in sections:
+        res["add_4096bit"] = add_section(args, ctx, dev, stream, world, rank)
+    if "ntt" in sections:
+        res["ntt_mul_65536bit"] = ntt_section(args, ctx, dev, stream, world, rank)
+    if "ragged" in sections:
+        res["ragged_200k"] = ragged_vs_plain(args, ctx, dev, stream, world, rank)
+    if "serving" in sections:
+        res["serving"] = serving_sweep(args, ctx, rank)
+    if "u32" in sections:
+        res["mul_8192bit_u32limbs"] = u32_section(args, ctx, dev, stream, world, rank)
+    return res
+
+
+def add_section(args, ctx, dev, stream, world, rank) -> dict:
     import torch
 
-    import midint
     import workloads
 
     sp = stream.cuda_stream
-    res = {}
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
-
+    hbm = measured_peaks().get("hbm_gbs")
     a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=workloads.SEED_BASE + 1000 * rank)
     set_bytes = 3 * a.nbytes + N_ADD
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
@@ -361,7 +377,7 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
     ms = max_over_ranks(world, time_device(add_step, sets, steps, max(args.warmup, 5), stream))
     algo_bytes = N_ADD * (3 * M_ADD * 8 + 1)
     gbs = algo_bytes / (ms * 1e-3) / 1e9
-    res["add_4096bit"] = {
+    out = {
         "config": "plain addition, 65536 pairs x 4096-bit (64 u64 limbs), every 8th pair all-ones + 1; "
                   "sum mod 2^4096 + carry-out byte",
         "ms_per_launch": ms, "GB/s": gbs * world, "instances/s": world * N_ADD / (ms * 1e-3),
@@ -372,8 +388,18 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
     }
     del da, db, dr, dc
+    torch.cuda.empty_cache()
+    return out
 
-    # NTT multiplication: 1024 pairs x 65536-bit, every 16th pair all ones
+
+def ntt_section(args, ctx, dev, stream, world, rank) -> dict:
+    """NTT multiplication: 1024 pairs x 65536-bit, every 16th pair all ones."""
+    import torch
+
+    import midint
+    import workloads
+
+    sp = stream.cuda_stream
     n_ntt, m_ntt = 1024, 1024
     a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, seed=workloads.SEED_BASE + 2 + 1000 * rank)
     set_bytes = 4 * a.nbytes
@@ -390,7 +416,7 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
     modmuls = 107520          # 3 primes x (3 transforms x 1024*11 butterflies + 2048 pointwise)
     pp_per_modmul = 6         # 4 partial products for x*y, 2 for the reduction (p = c*2^32 + 1)
     achieved = n_ntt * modmuls * pp_per_modmul / (ms * 1e-3)
-    res["ntt_mul_65536bit"] = {
+    out = {
         "config": "plain NTT multiplication, 1024 pairs x 65536-bit (1024 u64 limbs) -> 131072-bit product, "
                   "every 16th pair all-ones; 3 primes < 2^62, 2048-point transforms, CRT + carry fused",
         "ms_per_launch": ms, "products/s": world * n_ntt / (ms * 1e-3),
@@ -401,10 +427,17 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
     }
     del da, db, dr
+    torch.cuda.empty_cache()
+    return out
 
-    res["ragged_200k"] = ragged_vs_plain(args, ctx, dev, stream, world, rank)
-    res["serving"] = serving_sweep(args, ctx, rank)
 
+def u32_section(args, ctx, dev, stream, world, rank) -> dict:
+    """The u32-limb variant of the classical multiplication (256 u32 limbs)."""
+    import torch
+
+    import workloads
+
+    sp = stream.cuda_stream
     # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
     a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
     with torch.cuda.stream(stream):
@@ -414,11 +447,11 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
     torch.cuda.synchronize()
     ms = max_over_ranks(world, time_device(
         lambda i: ctx.mul_full(da, db, dr, N_MUL, 2 * M_MUL, limb_bits=32, stream=sp), 1, 20, 3, stream))
-    res["mul_8192bit_u32limbs"] = {"ms_per_launch": ms, "products/s": world * N_MUL / (ms * 1e-3),
-                                   "note": "operands L2-resident between launches (single set)"}
+    out = {"ms_per_launch": ms, "products/s": world * N_MUL / (ms * 1e-3),
+           "note": "operands L2-resident between launches (single set)"}
     del da, db, dr
     torch.cuda.empty_cache()
-    return res
+    return out
 
 
 def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
@@ -432,7 +465,7 @@ def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     import workloads
     from plainform import PlainBatch
 
-    ops, pool, out_limbs = workloads.ragged_ops(seed=workloads.SEED_BASE + 3 + 1000 * rank)
+    ops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops, seed=workloads.SEED_BASE + 3 + 1000 * rank)
     n = ops.size
     sp = stream.cuda_stream
     with torch.cuda.stream(stream):
@@ -468,7 +501,7 @@ def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     if not same:
         raise SystemExit("bench: ragged and plain-form results differ")
     return {
-        "config": "200000 ops, 40% add / 60% mul, operand bits log-uniform in [256, 65536] (4..1024 u64 limbs), "
+        "config": f"{n} ops, 40% add / 60% mul, operand bits log-uniform in [256, 65536] (4..1024 u64 limbs), "
                   "independent lengths; adds return max(la,lb) limbs + carry, muls la+lb limbs",
         "ragged_ms": ms_r, "ragged_ops/s": world * n / (ms_r * 1e-3),
         "plain_ms": ms_p, "plain_ops/s": world * n / (ms_p * 1e-3), "plain_launches": launches[0],
