@@ -212,6 +212,21 @@ mi_status mi_ragged_run(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
 /* Number of ops the last run on this scratch skipped as invalid (synchronous). */
 mi_status mi_ragged_invalid(const void* scratch, uint32_t* count);
 
+/* The ragged run of mi_ragged_run for callers that cannot allocate device
+ * memory -- code that runs inside another framework's memory pool or under a
+ * fixed device-memory budget, where a cudaMalloc would fail or is not
+ * allowed.  It allocates nothing: its scratch is a static device array of the
+ * library sized for at most MI_RAGGED_NOALLOC_MAX_OPS ops (about 0.5 MiB, held
+ * by every GPU that loads the library until the process exits); larger lists
+ * are refused with MI_EINVAL.  The first call on a device looks the array up
+ * (and loads the size-class tables); make it before capturing any stream.
+ * All calls share the array, so calls whose work overlaps on the GPU race:
+ * order them on one stream.  The context is created beforehand as usual.
+ * No counterpart in the reference. */
+#define MI_RAGGED_NOALLOC_MAX_OPS 65536u
+mi_status mi_ragged_run_noalloc(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
+                                uint8_t* carry_out, mi_stream stream);
+
 /* The same run captured once into a CUDA graph and replayed. */
 typedef struct mi_graph_s* mi_graph;
 mi_status mi_ragged_graph_create(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,

@@ -465,6 +465,61 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
 
 size_t ragged_scratch_words(uint32_t n_ops) { return rg::Scratch::words(n_ops); }
 mi_status ragged_prepare() { return rg::init_device(); }
+
+// --- the allocation-free variant ---------------------------------------------------
+//
+// Scratch for callers that cannot allocate device memory: a file-scope device
+// array sized for at most MI_RAGGED_NOALLOC_MAX_OPS ops (about 0.5 MiB, held by
+// every GPU that loads the library until the process exits).  In host code
+// `g_noalloc_scratch` names a host-side stand-in, not device memory; the device
+// address comes from cudaGetSymbolAddress, once per device, with that device
+// current, on the first call there.
+namespace rg {
+static __device__ __align__(256) uint32_t g_noalloc_scratch[Scratch::words(MI_RAGGED_NOALLOC_MAX_OPS)];
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+mi_status noalloc_scratch(void** out) {
+    int dev = 0;
+    MI_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(MI_ENODEV, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(noalloc scratch)");
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return MI_OK;
+}
+}  // namespace rg
+
+}  // namespace mi
+
+// Same work as mi_ragged_run, for callers that cannot allocate device memory
+// (for example code that runs inside another framework's memory pool, or under
+// a fixed device-memory budget, where a cudaMalloc would fail or is not
+// allowed): the scratch is the library's static device array instead of a
+// caller buffer.  No allocation, no free, no allocating library routine.
+extern "C" mi_status mi_ragged_run_noalloc(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in,
+                                           uint64_t* out, uint8_t* carry_out, mi_stream stream) {
+    using namespace mi;
+    if (ctx == nullptr) return set_error(MI_EINVAL, "ragged_run_noalloc: null context");
+    if (n_ops > MI_RAGGED_NOALLOC_MAX_OPS)
+        return set_error(MI_EINVAL, "ragged_run_noalloc: %u ops exceed the static scratch limit of %u ops", n_ops,
+                         MI_RAGGED_NOALLOC_MAX_OPS);
+    if (n_ops == 0) return MI_OK;
+    int cur = -1;
+    MI_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != ctx->device) MI_CUDA_TRY(cudaSetDevice(ctx->device));
+    void* scratch = nullptr;
+    MI_TRY(rg::noalloc_scratch(&scratch));
+    return ragged_launch(ctx, ops, n_ops, in, out, carry_out, scratch, rg::Scratch::words(MI_RAGGED_NOALLOC_MAX_OPS) * 4,
+                         ctx->ragged_ntt_min, reinterpret_cast<cudaStream_t>(stream));
+}
+
+namespace mi {
 size_t ragged_invalid_word() { return rg::Scratch::INVALID; }
 
 }  // namespace mi

@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(HERE, "libmidint_gb300.so")
 
 MI_OK, MI_EINVAL, MI_ENOMEM, MI_ECUDA, MI_ETIMEOUT, MI_ENODEV, MI_ENOTSUP = range(7)
 MAX_LIMBS_U64 = 1024
+RAGGED_NOALLOC_MAX_OPS = 65536
 
 # Every symbol include/midint.h declares, with (restype, argtypes).
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
@@ -62,6 +63,7 @@ SIGNATURES = {
     "mi_ragged_scratch_bytes": (_S, [_U32, ctypes.POINTER(ctypes.c_size_t)]),
     "mi_ragged_run": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "mi_ragged_invalid": (_S, [_P, ctypes.POINTER(_U32)]),
+    "mi_ragged_run_noalloc": (_S, [_P, _P, _U32, _P, _P, _P, _P]),
     "mi_ragged_graph_create": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)]),
     "mi_graph_launch": (_S, [_P, _P]),
     "mi_graph_destroy": (_S, [_P]),
@@ -202,6 +204,11 @@ class Context:
         """Runs a ragged list of mi_op records (device array) on the device."""
         check(load().mi_ragged_run(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out), _ptr(carry),
                                    _ptr(scratch), scratch_bytes, _ptr(stream)))
+
+    def ragged_run_noalloc(self, ops, n_ops: int, pool_in, pool_out, carry=None, stream=None) -> None:
+        """The ragged run on the library's static scratch (no device allocation)."""
+        check(load().mi_ragged_run_noalloc(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out), _ptr(carry),
+                                           _ptr(stream)))
 
     def ragged_graph(self, ops, n_ops: int, pool_in, pool_out, scratch, scratch_bytes: int, carry=None) -> "Graph":
         h = ctypes.c_void_p()
