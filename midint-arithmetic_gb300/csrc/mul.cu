@@ -41,8 +41,7 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
     const uint32_t t = threadIdx.x % NT;
     uint32_t* gA = sA + grp * S::WPAD;
     uint4* gB4 = reinterpret_cast<uint4*>(sB + grp * S::WPAD);
-    uint32_t* mine = sT + threadIdx.x * classic::PER_T;
-    const uint32_t* gT = sT + grp * NT * classic::PER_T;
+    uint2* slots = reinterpret_cast<uint2*>(sT) + grp * NT * classic::PAIRS;
     uint32_t* scr = sA;  // only used after the tile loop, by groups wider than a warp
     const uint32_t rlen = full ? 2 * n32 : n32;
     const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
@@ -57,7 +56,7 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
         classic::stage_b<NT, VEC>(gB4, b + off, n32, valid, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT>(gA, gB4, mine, gT, scr, t, ulo, uhi);
+        classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi);
         if (valid) {
             uint32_t* rr = r + inst * rlen;
             classic::store_block<VEC>(rr, t * T, rlen, ulo);

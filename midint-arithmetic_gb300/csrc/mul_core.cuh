@@ -49,9 +49,13 @@ struct DiagAcc {
     static constexpr int WORDS = 2 * T + 2 * T - 2 + T + 1;  // 39
 };
 
-constexpr int ACC = 2 * T + 1;                  // words of a folded anti-diagonal value
-constexpr int SNAP = 4 * ((DiagAcc::WORDS + 3) / 4);
-constexpr int PER_T = SNAP > 2 * ACC ? SNAP : 2 * ACC;  // shared words per thread (40)
+constexpr int ACC = 2 * T + 1;  // words of a folded anti-diagonal value
+// Shared memory per thread, in 64-bit pairs, laid out [pair][thread of the
+// group] so that a thread's own pairs and its neighbours' pairs are read by
+// consecutive threads at consecutive 8-byte slots (no bank conflicts).  Holds
+// either the snapshot of a DiagAcc (8 + 7 + 5 pairs) or D1, D2 (2 x 17 words).
+constexpr int PAIRS = 20;
+constexpr int PER_T = 2 * PAIRS;  // words per thread (40)
 
 __device__ __forceinline__ void tile_mac(const uint32_t (&A)[T], const uint32_t (&B)[T], DiagAcc& s) {
 #pragma unroll
@@ -141,13 +145,14 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 
 // The full product of the group's staged A (NT blocks) and B (NT blocks).
 // On return thread t holds output blocks t (lo, limbs tT..tT+T-1) and t+NT
-// (hi), fully carried.  `mine` is the thread's PER_T shared words, `gT` the
-// group's first thread's, `scr` per-warp scratch for groups wider than a warp.
-// Starts and ends with the group's shared areas free for reuse by the caller
-// after a group_sync.
+// (hi), fully carried.  `slots` is the group's PAIRS*NT 64-bit shared slots
+// (pair w of thread l at slots[w*NT + l]), `scr` per-warp scratch for groups
+// wider than a warp.  Starts and ends with the group's shared areas free for
+// reuse by the caller after a group_sync.
 template <int NT>
-__device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint32_t* mine, const uint32_t* gT,
-                                               uint32_t* scr, uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+__device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
+                                               uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+    auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NT + lane]; };
     DiagAcc s;
 #pragma unroll
     for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
@@ -169,30 +174,27 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
         tile_mac(A, B, s);
         if (k == t) {
-            // anti-diagonal t is complete: snapshot the accumulator
-            uint32_t tmp[SNAP];
+            // anti-diagonal t is complete: snapshot the accumulator, straight
+            // from its register pairs
 #pragma unroll
-            for (int w = 0; w < 2 * T; ++w) tmp[w] = s.a[w];
+            for (int w = 0; w < T; ++w) slot(w, t) = make_uint2(s.a[2 * w], s.a[2 * w + 1]);
 #pragma unroll
-            for (int w = 0; w < 2 * T - 2; ++w) tmp[2 * T + w] = s.b[w];
+            for (int w = 0; w < T - 1; ++w) slot(T + w, t) = make_uint2(s.b[2 * w], s.b[2 * w + 1]);
 #pragma unroll
-            for (int w = 0; w < T + 1; ++w) tmp[4 * T - 2 + w] = s.cc[w];
-#pragma unroll
-            for (int w = DiagAcc::WORDS; w < SNAP; ++w) tmp[w] = 0;
-#pragma unroll
-            for (int q = 0; q < SNAP / 4; ++q)
-                reinterpret_cast<uint4*>(mine)[q] = make_uint4(tmp[4 * q], tmp[4 * q + 1], tmp[4 * q + 2], tmp[4 * q + 3]);
+            for (int w = 0; w < T / 2; ++w) slot(2 * T - 1 + w, t) = make_uint2(s.cc[2 * w], s.cc[2 * w + 1]);
+            slot(2 * T - 1 + T / 2, t) = make_uint2(s.cc[T], 0u);
         }
     }
 
     // split into the two anti-diagonal values D1 (s=t) and D2 (s=t+NT)
     uint32_t d1[ACC], d2[ACC];
     {
-        uint32_t snap[SNAP];
+        uint32_t snap[2 * PAIRS];
 #pragma unroll
-        for (int q = 0; q < SNAP / 4; ++q) {
-            const uint4 v = reinterpret_cast<const uint4*>(mine)[q];
-            snap[4 * q] = v.x; snap[4 * q + 1] = v.y; snap[4 * q + 2] = v.z; snap[4 * q + 3] = v.w;
+        for (int w = 0; w < PAIRS; ++w) {
+            const uint2 v = slot(w, t);
+            snap[2 * w] = v.x;
+            snap[2 * w + 1] = v.y;
         }
         fold(snap, snap + 2 * T, snap + 4 * T - 2, d1);
         fold(s.a, s.b, s.cc, d2);
@@ -200,16 +202,22 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
 #pragma unroll
         for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
         subc(d2[ACC - 1], d1[ACC - 1]);
+        // D1 words 0..16 in pairs 0..8, D2 words in pairs 9..17
 #pragma unroll
-        for (int w = 0; w < ACC; ++w) {
-            mine[w] = d1[w];
-            mine[ACC + w] = d2[w];
+        for (int w = 0; w < ACC / 2; ++w) {
+            slot(w, t) = make_uint2(d1[2 * w], d1[2 * w + 1]);
+            slot(9 + w, t) = make_uint2(d2[2 * w], d2[2 * w + 1]);
         }
+        slot(ACC / 2, t) = make_uint2(d1[ACC - 1], 0u);
+        slot(9 + ACC / 2, t) = make_uint2(d2[ACC - 1], 0u);
     }
     group_sync<NT>();
 
     // output blocks s=t (lo) and s=t+NT (hi): L_s + H_(s-1) + O_(s-2)
-    auto peer = [&](uint32_t lane, int which, int w) -> uint32_t { return gT[lane * PER_T + which * ACC + w]; };
+    auto peer = [&](uint32_t lane, int which, int w) -> uint32_t {
+        const uint2 v = slot(which * 9 + w / 2, lane);
+        return (w & 1) ? v.y : v.x;
+    };
     uint32_t Hlo[T], Hhi[T], Olo = 0, Ohi = 0;
 #pragma unroll
     for (int w = 0; w < T; ++w) {

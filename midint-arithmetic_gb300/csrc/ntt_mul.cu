@@ -39,8 +39,9 @@ struct NttShape {
     static constexpr size_t SMEM = ntt::MulSmem<LG>::WORDS64 * 8 + size_t(NT / 32 + 1) * 4;
 };
 
+// 768 threads per SM: three 256-thread CTAs for 2048-point transforms
 template <int LG>
-__global__ void __launch_bounds__((1 << LG) / 8)
+__global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     k_ntt_mul(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ r, uint32_t n,
               uint32_t m, uint32_t rlen, NttMulParams P) {
     extern __shared__ __align__(16) uint64_t smem[];

@@ -39,26 +39,41 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
                                         uint64_t* sm, uint32_t* scr) {
     using Pl = Plan<LG>;
-    uint64_t* sh = sm;
+    uint64_t* sh = sm;           // exchange buffer
     uint64_t* res = sm + Pl::L;  // res[q][slot], q < 3
+    // a's spectrum waits in res[2]'s region: it is read back (by the thread
+    // that wrote it) before the inverse transform of the last prime, whose
+    // barriers order those reads before res[2] is written.
+    uint64_t* spec = res + 2 * Pl::L;
     const uint32_t t = threadIdx.x % Pl::NT;
 #pragma unroll 1
     for (int q = 0; q < 3; ++q) {
         const FieldC32 f{P.p[q], 2 * P.p[q], P.c[q]};
         const uint64_t ka = P.ka_by_lg[q][LG];
-        uint64_t x[8], y[8];
+        uint64_t x[8];
+        // a*(R/L)/R = a/L and b*R^2/R = b*R: the pointwise product is then
+        // a*b/L in plain form and the inverse needs no scaling.
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
-            // a*(R/L)/R = a/L and b*R^2/R = b*R: the pointwise product is
-            // then a*b/L in plain form and the inverse needs no scaling.
             x[j] = (i < la) ? f.mul(__ldg(ar + i), ka) : 0;
-            y[j] = (i < lb) ? f.mul(__ldg(br + i), P.kb[q]) : 0;
         }
         forward<LG>(x, sh, P.tw[q], f);
-        forward<LG>(y, sh, P.tw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = f.mul(x[j], y[j]);
+        for (int j = 0; j < 8; j += 2)
+            *reinterpret_cast<ulonglong2*>(spec + swz(8 * t + j)) = make_ulonglong2(x[j], x[j + 1]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t i = t + Pl::NT * j;
+            x[j] = (i < lb) ? f.mul(__ldg(br + i), P.kb[q]) : 0;
+        }
+        forward<LG>(x, sh, P.tw[q], f);
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(spec + swz(8 * t + j));
+            x[j] = f.mul(x[j], v.x);
+            x[j + 1] = f.mul(x[j + 1], v.y);
+        }
         inverse<LG>(x, sh, P.itw[q], f);
 #pragma unroll
         for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = reduce1(x[j], f.p);

@@ -227,7 +227,7 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint64
     }
 }
 
-__global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
+__global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
     extern __shared__ __align__(16) uint64_t smem[];
     uint32_t* scr_warp = reinterpret_cast<uint32_t*>(smem + 8192);  // after 64 KiB
     __shared__ uint32_t s_task;
@@ -261,9 +261,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     const mi_op op = P.ops[sorted[tk.first + g]];
     uint32_t* gA = wsm + g * NT * T;
     uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g * 2 * NT;
-    uint32_t* slots = wsm + 512;
-    uint32_t* mine = slots + lane * classic::PER_T;
-    const uint32_t* gT = slots + g * NT * classic::PER_T;
+    uint2* slots = reinterpret_cast<uint2*>(wsm + 512) + g * NT * classic::PAIRS;
     // longer operand x is consumed in chunks of W limbs against the staged shorter y
     const bool a_long = op.la >= op.lb;
     const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
@@ -281,7 +279,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         classic::stage_a<NT, false>(gA, x + c * W, left < W ? left : W, true, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT>(gA, gB4, mine, gT, nullptr, t, ulo, uhi);
+        classic::square_product<NT>(gA, gB4, slots, nullptr, t, ulo, uhi);
         // limbs [cW, (c+1)W) are final: the low half plus the pending window
         uint32_t fin[T];
         bool g0, p0;
