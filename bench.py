@@ -57,8 +57,8 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
     ap.add_argument("--ragged-ops", type=int, default=200000, help="ops in the ragged batch")
-    ap.add_argument("--sections", default="add,ntt,ragged,serving,u32",
-                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32)")
+    ap.add_argument("--sections", default="add,ntt,ragged,serving,u32,fused",
+                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused)")
     return ap.parse_args()
 
 
@@ -92,14 +92,26 @@ def barrier(world):
 
 
 def max_over_ranks(world, x: float) -> float:
+    """The largest x over all ranks (a step time: the job ends with its slowest rank)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_seed(base: int, rank: int) -> int:
+    """Seed of a rank's own batch: ranks process disjoint instances (weak scaling)."""
+    return base + 1000 * rank
+
+
+def job_rate(world: int, units_per_rank: int, max_ms: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / (max_ms * 1e-3)
 
 
 # --- clocks ----------------------------------------------------------------------
@@ -242,7 +254,7 @@ def run_ours(args):
     sp = stream.cuda_stream
 
     # --- headline: classical multiplication, device-resident operands ---------
-    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
     in_bytes = a.nbytes
     set_bytes = 2 * in_bytes + 2 * in_bytes
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
@@ -268,7 +280,7 @@ def run_ours(args):
     ms = time_device(mul_step, sets, args.steps, args.warmup, stream)
     clk = clocks.stop()
     ms = max_over_ranks(world, ms)
-    products_s = world * N_MUL / (ms * 1e-3)
+    products_s = job_rate(world, N_MUL, ms)
     prods32_per_inst = (2 * M_MUL) ** 2
     achieved_prod = N_MUL * prods32_per_inst / (ms * 1e-3)
 
@@ -350,6 +362,8 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         res["serving"] = serving_sweep(args, ctx, rank)
     if "u32" in sections:
         res["mul_8192bit_u32limbs"] = u32_section(args, ctx, dev, stream, world, rank)
+    if "fused" in sections:
+        res["fused"] = fused_section(args, ctx, dev, stream, world, rank)
     return res
 
 
@@ -360,7 +374,7 @@ def add_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     hbm = measured_peaks().get("hbm_gbs")
-    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=workloads.SEED_BASE + 1000 * rank)
+    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=rank_seed(workloads.SEED_BASE, rank))
     set_bytes = 3 * a.nbytes + N_ADD
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
     with torch.cuda.stream(stream):
@@ -401,7 +415,7 @@ def ntt_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     n_ntt, m_ntt = 1024, 1024
-    a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, seed=workloads.SEED_BASE + 2 + 1000 * rank)
+    a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, seed=rank_seed(workloads.SEED_BASE + 2, rank))
     set_bytes = 4 * a.nbytes
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
     with torch.cuda.stream(stream):
@@ -439,7 +453,7 @@ def u32_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
-    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=workloads.SEED_BASE + 1 + 1000 * rank)
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
     with torch.cuda.stream(stream):
         da = torch.from_numpy(a.view(np.int64)).to(dev)
         db = torch.from_numpy(b.view(np.int64)).to(dev)
@@ -454,6 +468,49 @@ def u32_section(args, ctx, dev, stream, world, rank) -> dict:
     return out
 
 
+def fused_section(args, ctx, dev, stream, world, rank) -> dict:
+    """The fused composites: 6a + 10b on the addition workload and
+    ((a^2 + b)(b^2 + b) + ab) mod 2^8192 on the multiplication workload."""
+    import torch
+
+    import workloads
+
+    sp = stream.cuda_stream
+    hbm = measured_peaks().get("hbm_gbs")
+    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=rank_seed(workloads.SEED_BASE, rank))
+    sets = max(2, -(-4 * L2_BYTES // (3 * a.nbytes)))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+    ms6 = max_over_ranks(world, time_device(
+        lambda i: ctx.add6(da[i], db[i], dr[i], N_ADD, M_ADD, stream=sp), sets, max(args.steps, 100),
+        max(args.warmup, 5), stream))
+    gbs = N_ADD * 3 * M_ADD * 8 / (ms6 * 1e-3) / 1e9
+    del da, db, dr
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
+    sets = max(2, -(-4 * L2_BYTES // (3 * a.nbytes)))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+    msp = max_over_ranks(world, time_device(
+        lambda i: ctx.poly(da[i], db[i], dr[i], N_MUL, M_MUL, stream=sp), sets, max(10, args.steps // 2),
+        max(args.warmup, 3), stream))
+    del da, db, dr
+    torch.cuda.empty_cache()
+    return {
+        "add6": {"config": "6a + 10b mod 2^4096, 65536 pairs x 64 u64 limbs (the addition workload)",
+                 "ms_per_launch": ms6, "instances/s": world * N_ADD / (ms6 * 1e-3), "GB/s": world * gbs,
+                 "frac_hbm": (gbs / hbm) if hbm else None},
+        "poly": {"config": "((a^2 + b)(b^2 + b) + ab) mod 2^8192, 16384 pairs x 128 u64 limbs "
+                           "(the multiplication workload); 4 products + 3 sums in one kernel",
+                 "ms_per_launch": msp, "instances/s": world * N_MUL / (msp * 1e-3)},
+    }
+
+
 def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     """Ragged batch of 200000 mixed ops: the persistent ragged kernels
     (replayed CUDA graph) against the plain per-size-class launches with both
@@ -465,7 +522,7 @@ def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     import workloads
     from plainform import PlainBatch
 
-    ops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops, seed=workloads.SEED_BASE + 3 + 1000 * rank)
+    ops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops, seed=rank_seed(workloads.SEED_BASE + 3, rank))
     n = ops.size
     sp = stream.cuda_stream
     with torch.cuda.stream(stream):
@@ -577,7 +634,7 @@ def serving_sweep(args, ctx, rank) -> dict:
 def workloads_seed(rank: int) -> int:
     import workloads
 
-    return workloads.SEED_BASE + 4 + 1000 * rank
+    return rank_seed(workloads.SEED_BASE + 4, rank)
 
 
 def run_reference(args):

@@ -119,6 +119,12 @@ mi_status mi_mul_full_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint
 mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r,
                           uint32_t n, uint32_t limbs, mi_stream stream);
 
+/* Fused polynomial composite r = ((a^2 + b)(b^2 + b) + ab) mod 2^(64*limbs),
+ * every intermediate mod 2^(64*limbs) and held on chip, limbs <= 1024.
+ * Replaces polyKerQ (cuda/ker-classic-mul.cu.h:500-575). */
+mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
+                      uint32_t n, uint32_t limbs, mi_stream stream);
+
 /* ---------------------------------------------------------------------------
  * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 1024: every u64
  * limb is one digit, three 62-bit primes (the first is the reference's

@@ -307,6 +307,18 @@ mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint
     return mul_any(ctx, a, b, r, n, limbs, stream, 4, true);
 }
 
+mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
+                      mi_stream stream) {
+    MI_TRY(check_batch(a, b, r, limbs, kMulMaxN32 / 2, "poly"));
+    const size_t bytes = size_t(n) * limbs * 8;
+    if (n > 0 && (any_overlap(r, bytes, a, bytes) || any_overlap(r, bytes, b, bytes)))
+        return set_error(MI_EINVAL, "poly: result overlaps an operand");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    return launch_poly(reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b),
+                       reinterpret_cast<uint32_t*>(r), n, 2 * limbs, pick_stream(ctx, stream));
+}
+
 mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                          mi_stream stream) {
     return mul_ntt(ctx, a, b, r, n, limbs, stream);

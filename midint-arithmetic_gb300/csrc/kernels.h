@@ -22,6 +22,9 @@ mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
                              bool full, cudaStream_t st);
 
+// ((a^2 + b)(b^2 + b) + ab) mod 2^(32*n32) per instance (u32 limb views).
+mi_status launch_poly(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st);
+
 // Ragged batches (ragged.cu): device scratch words for n_ops, the word that
 // counts skipped ops, the one-time per-device setup (call outside stream
 // capture) and the asynchronous launch sequence.

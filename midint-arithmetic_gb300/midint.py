@@ -57,6 +57,7 @@ SIGNATURES = {
     "mi_host_mul_full_u64": (_S, [_P, _P, _P, _P, _U32, _U32]),
     "mi_calib_mul32_peak": (_S, [_U32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "mi_mul_ntt_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
+    "mi_poly_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_mul_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_compat_gpuMulFFT_u16": (_S, [_I, _U32, _P, _P, _P]),
     "mi_ntt_raw": (_S, [ctypes.c_uint64, ctypes.c_uint64, _U32, _U32, _I, _P, _P, _P]),
@@ -189,6 +190,10 @@ class Context:
     def mul_full(self, a, b, r, n: int, limbs: int, limb_bits: int = 64, stream=None) -> None:
         f = load().mi_mul_full_u64 if limb_bits == 64 else load().mi_mul_full_u32
         check(f(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
+
+    def poly(self, a, b, r, n: int, limbs: int, stream=None) -> None:
+        """((a^2 + b)(b^2 + b) + ab) mod 2^(64*limbs), fused (u64 limbs)."""
+        check(load().mi_poly_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
 
     def mul_ntt(self, a, b, r, n: int, limbs: int, stream=None) -> None:
         """Exact full product by NTT (u64 limbs, limbs <= 1024)."""

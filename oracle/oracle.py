@@ -39,6 +39,7 @@ def lib() -> ctypes.CDLL:
         L.orc_add_u64.argtypes = [u64, u32, P, P, P, P]
         L.orc_add_u32.argtypes = [u64, u32, P, P, P, P]
         L.orc_add6_u64.argtypes = [u64, u32, P, P, P]
+        L.orc_poly_u64.argtypes = [u64, u32, P, P, P]
         L.orc_mul_u64.argtypes = [u64, u32, P, P, P, i32]
         L.orc_mul_u32.argtypes = [u64, u32, P, P, P, i32]
         for f in ("orc_zmod_mul", "orc_zmod_add", "orc_zmod_sub", "orc_zmod_pow"):
@@ -88,6 +89,14 @@ def add6(a: np.ndarray, b: np.ndarray, m: int) -> np.ndarray:
     a, b = _c(a, np.uint64), _c(b, np.uint64)
     r = np.empty_like(a)
     lib().orc_add6_u64(a.size // m, m, _p(a), _p(b), _p(r))
+    return r
+
+
+def poly(a: np.ndarray, b: np.ndarray, m: int) -> np.ndarray:
+    """((a^2 + b)(b^2 + b) + ab) mod 2^(64m) per instance (u64 limbs)."""
+    a, b = _c(a, np.uint64), _c(b, np.uint64)
+    r = np.empty_like(a)
+    lib().orc_poly_u64(a.size // m, m, _p(a), _p(b), _p(r))
     return r
 
 

@@ -159,6 +159,26 @@ void orc_mul_u32(uint64_t n, uint32_t m, const uint32_t* a, const uint32_t* b, u
     free(tmp);
 }
 
+/* (a^2 + b)(b^2 + b) + ab mod 2^(64m): the composite of polyKerQ
+ * (cuda/ker-classic-mul.cu.h:500-575) -- t1 = a*a, t2 = t1 + b, t3 = b*b,
+ * t4 = t3 + b, t5 = t2*t4, t6 = a*b, r = t5 + t6, every step mod 2^(64m). */
+void orc_poly_u64(uint64_t n, uint32_t m, const uint64_t* a, const uint64_t* b, uint64_t* r) {
+    uint64_t* t = (uint64_t*)malloc(sizeof(uint64_t) * m * 6);
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t* x = a + i * m;
+        const uint64_t* y = b + i * m;
+        uint64_t *t1 = t, *t2 = t + m, *t3 = t + 2 * m, *t4 = t + 3 * m, *t5 = t + 4 * m, *t6 = t + 5 * m;
+        orc_mul_u64(1, m, x, x, t1, 0);
+        orc_add_u64(1, m, t1, y, t2, NULL);
+        orc_mul_u64(1, m, y, y, t3, 0);
+        orc_add_u64(1, m, t3, y, t4, NULL);
+        orc_mul_u64(1, m, t2, t4, t5, 0);
+        orc_mul_u64(1, m, x, y, t6, 0);
+        orc_add_u64(1, m, t5, t6, r + i * m, NULL);
+    }
+    free(t);
+}
+
 /* ------------------------------------------------------------------------
  * Prime-field NTT primitives of the reference (cuda/ker-fft-mul.cu.h):
  * zmod_t add/sub/mul/pow/inv (:76-140) over a prime p < 2^63, getOmega /

@@ -93,6 +93,9 @@ def test_oracle_vs_python_ints(m):
     assert np.array_equal(O.mul(a32, b32, 2 * m, True).view(np.uint64), O.py_mul(a, b, m, True))
     assert np.array_equal(O.add6(a, b, m), O.from_ints([(6 * x + 10 * y) % (1 << (64 * m))
                                                         for x, y in zip(O.to_ints(a, m), O.to_ints(b, m))], m))
+    mod = 1 << (64 * m)
+    want = [((x * x + y) * (y * y + y) + x * y) % mod for x, y in zip(O.to_ints(a, m), O.to_ints(b, m))]
+    assert np.array_equal(O.poly(a, b, m), O.from_ints(want, m))
 
 
 def test_gmp_path_matches_restatement():
