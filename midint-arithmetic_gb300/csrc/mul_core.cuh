@@ -272,6 +272,157 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
     }
 }
 
+// Stages `n32` limbs of an operand row in the two-plane layout of NB blocks
+// (half h of block j at 16-byte slot h*NB + j), zero padded to NB*T limbs, by
+// THREADS threads.
+template <int NB, int THREADS, bool VEC>
+__device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restrict__ row, uint32_t n32, bool valid,
+                                             uint32_t t) {
+#pragma unroll
+    for (int it = 0; it < 2 * NB / THREADS; ++it) {
+        const uint32_t v = t + uint32_t(it) * THREADS;
+        uint4 q = make_uint4(0, 0, 0, 0);
+        if (VEC && valid && v * 4 + 4 <= n32) {
+            q = __ldcs(reinterpret_cast<const uint4*>(row) + v);
+        } else if (valid) {
+            const uint32_t w = v * 4;
+            if (w + 0 < n32) q.x = __ldcs(row + w + 0);
+            if (w + 1 < n32) q.y = __ldcs(row + w + 1);
+            if (w + 2 < n32) q.z = __ldcs(row + w + 2);
+            if (w + 3 < n32) q.w = __ldcs(row + w + 3);
+        }
+        g4[(v & 1) * NB + (v >> 1)] = q;
+    }
+}
+
+// The low NB = 2*NH blocks of the product of A and B (NB blocks each, both in
+// the two-plane layout).  Only the anti-diagonals s < NB are needed; thread t
+// of a group of NH threads owns s = t (t+1 tiles) and its mirror
+// s = NB-1-t (NB-t tiles): NB+1 tiles for every thread, the reference's
+// column pairing (cuda/ker-classic-mul.cu.h:406-423) at tile granularity.  In
+// the first t+1 steps thread t walks anti-diagonal t (A-block k broadcast,
+// B-block t-k); then its mirror (A-block k-t-1, B-block NB-k broadcast).  On
+// return thread t holds output blocks t (ulo) and NH+t (uhi), fully carried;
+// the carry out of block NB-1 is dropped (the product mod 2^(32*T*NB)).
+template <int NH>
+__device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
+                                            uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+    constexpr uint32_t NB = 2 * NH;
+    auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NH + lane]; };
+    DiagAcc s;
+#pragma unroll
+    for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
+#pragma unroll
+    for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
+#pragma unroll
+    for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+#pragma unroll 2
+    for (uint32_t k = 0; k <= NB; ++k) {
+        const bool first = k <= t;
+        const uint32_t i = first ? k : k - t - 1;
+        const uint32_t j = first ? t - k : NB - k;
+        uint32_t A[T], B[T];
+        const uint4 a0 = gA4[i];
+        const uint4 a1 = gA4[NB + i];
+        const uint4 b0 = gB4[j];
+        const uint4 b1 = gB4[NB + j];
+        A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
+        A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
+        B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
+        B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
+        tile_mac(A, B, s);
+        if (k == t) {
+#pragma unroll
+            for (int w = 0; w < T; ++w) slot(w, t) = make_uint2(s.a[2 * w], s.a[2 * w + 1]);
+#pragma unroll
+            for (int w = 0; w < T - 1; ++w) slot(T + w, t) = make_uint2(s.b[2 * w], s.b[2 * w + 1]);
+#pragma unroll
+            for (int w = 0; w < T / 2; ++w) slot(2 * T - 1 + w, t) = make_uint2(s.cc[2 * w], s.cc[2 * w + 1]);
+            slot(2 * T - 1 + T / 2, t) = make_uint2(s.cc[T], 0u);
+        }
+    }
+
+    // D1 = anti-diagonal t (the snapshot), D2 = anti-diagonal NB-1-t
+    {
+        uint32_t d1[ACC], d2[ACC];
+        uint32_t snap[2 * PAIRS];
+#pragma unroll
+        for (int w = 0; w < PAIRS; ++w) {
+            const uint2 v = slot(w, t);
+            snap[2 * w] = v.x;
+            snap[2 * w + 1] = v.y;
+        }
+        fold(snap, snap + 2 * T, snap + 4 * T - 2, d1);
+        fold(s.a, s.b, s.cc, d2);
+        sub_cc(d2[0], d1[0]);
+#pragma unroll
+        for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
+        subc(d2[ACC - 1], d1[ACC - 1]);
+#pragma unroll
+        for (int w = 0; w < ACC / 2; ++w) {
+            slot(w, t) = make_uint2(d1[2 * w], d1[2 * w + 1]);
+            slot(9 + w, t) = make_uint2(d2[2 * w], d2[2 * w + 1]);
+        }
+        slot(ACC / 2, t) = make_uint2(d1[ACC - 1], 0u);
+        slot(9 + ACC / 2, t) = make_uint2(d2[ACC - 1], 0u);
+    }
+    group_sync<NH>();
+
+    // word w of anti-diagonal value D_s (s < NB): thread s holds it as D1 for
+    // s < NH, thread NB-1-s as D2 otherwise
+    auto diag = [&](uint32_t sd, int w) -> uint32_t {
+        const bool low = sd < NH;
+        const uint2 v = slot((low ? 0 : 9) + w / 2, low ? sd : NB - 1 - sd);
+        return (w & 1) ? v.y : v.x;
+    };
+    // output block q: L_q + H_(q-1) + O_(q-2)
+    uint32_t Llo[T], Lhi[T], Hlo[T], Hhi[T];
+    const uint32_t qh = NH + t;
+#pragma unroll
+    for (int w = 0; w < T; ++w) {
+        Llo[w] = diag(t, w);
+        Lhi[w] = diag(qh, w);
+        Hlo[w] = (t >= 1) ? diag(t - 1, T + w) : 0u;
+        Hhi[w] = diag(qh - 1, T + w);
+    }
+    const uint32_t Olo = (t >= 2) ? diag(t - 2, 2 * T) : 0u;
+    const uint32_t Ohi = (qh >= 2) ? diag(qh - 2, 2 * T) : 0u;
+    {
+        bool g0, p0, g1, p1;
+        uint32_t c0, c1;
+        chunk_add<uint32_t, T>(Llo, Hlo, ulo, g0, p0);
+        chunk_add<uint32_t, T>(Lhi, Hhi, uhi, g1, p1);
+        const uint32_t cl = group_carry<NH>(g0, p0, 0u, &c0, scr);
+        const uint32_t ch = group_carry<NH>(g1, p1, c0, &c1, scr);
+        chunk_inc<uint32_t, T>(ulo, cl);
+        chunk_inc<uint32_t, T>(uhi, ch);
+    }
+    {
+        uint32_t Zlo[T], Zhi[T];
+#pragma unroll
+        for (int w = 0; w < T; ++w) {
+            Zlo[w] = 0;
+            Zhi[w] = 0;
+        }
+        Zlo[0] = Olo;
+        Zhi[0] = Ohi;
+        uint32_t vlo[T], vhi[T];
+        bool g0, p0, g1, p1;
+        uint32_t c0, c1;
+        chunk_add<uint32_t, T>(ulo, Zlo, vlo, g0, p0);
+        chunk_add<uint32_t, T>(uhi, Zhi, vhi, g1, p1);
+        const uint32_t cl = group_carry<NH>(g0, p0, 0u, &c0, scr);
+        const uint32_t ch = group_carry<NH>(g1, p1, c0, &c1, scr);
+        chunk_inc<uint32_t, T>(vlo, cl);
+        chunk_inc<uint32_t, T>(vhi, ch);
+#pragma unroll
+        for (int w = 0; w < T; ++w) {
+            ulo[w] = vlo[w];
+            uhi[w] = vhi[w];
+        }
+    }
+}
+
 // Stores the T limbs of `v` at limb o of a result row, clipped to rlen.
 template <bool VEC>
 __device__ __forceinline__ void store_block(uint32_t* rr, uint32_t o, uint32_t rlen, const uint32_t (&v)[T]) {
