@@ -123,6 +123,24 @@ __device__ __forceinline__ uint32_t group_add(const L (&x)[Q], const L (&y)[Q], 
     return gc;
 }
 
+// The value v of thread t-1 of the group (0 for t == 0).  Groups wider than a
+// warp pass the last lane's value through one shared word per warp.
+template <int GS>
+__device__ __forceinline__ uint64_t group_shift_up(uint64_t v, uint32_t t, uint64_t* xs) {
+    if constexpr (GS <= 32) {
+        const uint64_t u = __shfl_up_sync(group_lanes<GS>(), v, 1, GS);
+        return t == 0 ? 0ull : u;
+    } else {
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+        const uint64_t u = __shfl_up_sync(MI_FULL_MASK, v, 1);
+        if (lane == 31) xs[warp] = v;
+        __syncthreads();
+        const uint64_t w = (lane == 0) ? ((t == 0) ? 0ull : xs[warp - 1]) : u;
+        __syncthreads();
+        return w;
+    }
+}
+
 template <typename L, int Q, int GS, bool VEC, int OP>
 __global__ void __launch_bounds__(GS > 256 ? GS : 256)
     k_add(const L* __restrict__ a, const L* __restrict__ b, L* __restrict__ r, uint8_t* __restrict__ carry,
@@ -130,6 +148,7 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
     constexpr int BLOCK = GS > 256 ? GS : 256;
     constexpr int IPB = BLOCK / GS;
     __shared__ uint32_t scratch[BLOCK / 32];
+    __shared__ uint64_t shift[OP == ADD_PLAIN ? 1 : BLOCK / 32];
     const uint32_t grp = threadIdx.x / GS;
     const uint32_t t = threadIdx.x % GS;
     const uint32_t start = t * Q;
@@ -146,14 +165,24 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
         if constexpr (OP == ADD_PLAIN) {
             gc = group_add<L, Q, GS>(x, y, s, scratch);
         } else {
-            // 6a + 10b by the chain of a6pb10Ker (cuda/ker-addition.cu.h:304-324).
-            L t1[Q], t2[Q], t3[Q], t4[Q], t5[Q];
-            group_add<L, Q, GS>(x, y, t1, scratch);   // t1 = a + b
-            group_add<L, Q, GS>(t1, t1, t2, scratch); // t2 = 2a + 2b
-            group_add<L, Q, GS>(t2, y, t3, scratch);  // t3 = 2a + 3b
-            group_add<L, Q, GS>(t3, t3, t4, scratch); // t4 = 4a + 6b
-            group_add<L, Q, GS>(t4, t3, t5, scratch); // t5 = 6a + 9b
-            gc = group_add<L, Q, GS>(t5, y, s, scratch); // r = 6a + 10b
+            // 6a + 10b mod 2^(64m), the value of a6pb10Ker's chain of six
+            // additions (cuda/ker-addition.cu.h:304-324) with one carry pass:
+            // per limb 6a_i + 10b_i = lo_i + hi_i*2^64 with hi_i <= 15, and
+            // the result is lo + (hi shifted up one limb), whose limb sums
+            // carry at most 1.
+            static_assert(sizeof(L) == 8, "6a + 10b is defined on u64 limbs");
+            L lo[Q], hi[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const L pa = x[q] * 6u, pb = y[q] * 10u;
+                lo[q] = pa + pb;
+                hi[q] = __umul64hi(x[q], 6u) + __umul64hi(y[q], 10u) + L(lo[q] < pa);
+            }
+            L sh[Q];
+            sh[0] = group_shift_up<GS>(hi[Q - 1], t, shift);
+#pragma unroll
+            for (int q = 1; q < Q; ++q) sh[q] = hi[q - 1];
+            gc = group_add<L, Q, GS>(lo, sh, s, scratch);
         }
         store_chunk<L, Q, VEC>(r + off, start, m, valid, s);
         if (OP == ADD_PLAIN && carry != nullptr && valid) {

@@ -104,7 +104,7 @@ def test_add_empty_batch(ctx, devmem):
     ctx.add(pa, pa, pa, 0, 8, stream=_stream())
 
 
-@pytest.mark.parametrize("m", [1, 4, 33, 64, 128, 1000])
+@pytest.mark.parametrize("m", [1, 2, 3, 4, 17, 33, 64, 65, 128, 1000, 2048, 4096])
 def test_add6_matches_oracle(ctx, devmem, m):
     n = 41
     a, b = carry_stress(n, m, seed=7 * m)
