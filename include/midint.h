@@ -84,6 +84,18 @@ mi_stream mi_ctx_stream(mi_ctx ctx);
  * (1..1025; 1025 = never).  Defaults come from the committed tuning table. */
 mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min);
 
+/* Tunable launch choices of a context.  A new context starts from the table
+ * that the project's autotuner measured and committed; these calls override
+ * one entry (the autotuner itself sweeps candidates through them).
+ *   MI_TUNE_PLAIN_NTT_MIN    cls ignored; value 1..1025 (as plain_ntt_min)
+ *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..129 (as ragged_ntt_min)
+ *   MI_TUNE_ADD_THREAD_BYTES cls = ceil(log2(u64 limbs)) 0..12 of the
+ *                            operands; value = bytes of each operand one
+ *                            thread owns: 16, 32 or 64 */
+enum { MI_TUNE_PLAIN_NTT_MIN = 0, MI_TUNE_RAGGED_NTT_MIN = 1, MI_TUNE_ADD_THREAD_BYTES = 2 };
+mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
+mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value);
+
 /* ---------------------------------------------------------------------------
  * Batched addition  r = (a + b) mod 2^(bits*limbs), carry_out[i] = carry bit.
  * Replaces baddKer<Base,IPB,M,Q> (cuda/ker-addition.cu.h:227-260) as launched

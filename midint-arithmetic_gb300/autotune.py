@@ -1,0 +1,215 @@
+"""Autotuner for the library's launch choices.
+
+Measures, on the GPU it runs on, every candidate of the tunable choices through
+the context's tuning override (`mi_ctx_set_tuning`) and writes
+
+  csrc/tuning_table.h   the defaults compiled into the library
+  tuning.json           the record: device, every candidate's time, the pick
+
+Knobs:
+  * addition, per size class c = ceil(log2(u64 limbs)), c = 0..12: operand bytes
+    per thread (16, 32 or 64), on batches of about 256 MiB of operands (twice
+    the L2) at the class's largest size;
+  * plain classical/NTT crossover of mi_mul_u64: both paths timed on square
+    products from 64 to 1024 u64 limbs; the crossover is the smallest measured
+    size from which the NTT is faster at every larger measured size;
+  * ragged classical/NTT crossover: the 200000-op mixed ragged workload (40%
+    adds, operand bits log-uniform in [256, 65536]) timed end to end for every
+    candidate threshold; the fastest wins.
+
+Usage:  python midint-arithmetic_gb300/autotune.py [--out-dir DIR] [--apply]
+(--apply writes into the package; otherwise into DIR, default the working
+directory, for review.)  Needs a CUDA device.
+"""
+from __future__ import annotations
+
+import argparse
+import datetime
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _timer(fn, reps: int, warmup: int, stream) -> float:
+    """Median over 3 rounds of the mean device time (ms) of `reps` calls."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    rounds = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        rounds.append(e0.elapsed_time(e1) / reps)
+    return float(np.median(rounds))
+
+
+def tune_add(ctx, stream, dev) -> tuple[list[int], dict]:
+    import torch
+
+    import midint
+
+    picks, record = [], {}
+    for c in range(13):
+        limbs = 1 << c
+        n = max(1024, (256 << 20) // (3 * 8 * limbs))
+        sets = 2
+        a = [torch.randint(-2**62, 2**62, (n * limbs,), dtype=torch.int64, device=dev) for _ in range(sets)]
+        b = [torch.randint(-2**62, 2**62, (n * limbs,), dtype=torch.int64, device=dev) for _ in range(sets)]
+        r = [torch.empty(n * limbs, dtype=torch.int64, device=dev) for _ in range(sets)]
+        cr = [torch.empty(n, dtype=torch.uint8, device=dev) for _ in range(sets)]
+        times = {}
+        for tb in (16, 32, 64):
+            ctx.set_tuning(midint.TUNE_ADD_THREAD_BYTES, c, tb)
+            it = [0]
+
+            def step():
+                i = it[0] % sets
+                it[0] += 1
+                ctx.add(a[i], b[i], r[i], n, limbs, carry=cr[i], stream=stream.cuda_stream)
+
+            ms = _timer(step, 20, 5, stream)
+            times[tb] = {"ms": ms, "GB/s": n * (3 * 8 * limbs + 1) / (ms * 1e-3) / 1e9}
+        best = min(times, key=lambda k: times[k]["ms"])
+        ctx.set_tuning(midint.TUNE_ADD_THREAD_BYTES, c, best)
+        picks.append(best)
+        record[f"class_{c}"] = {"u64_limbs": limbs, "instances": n, "candidates": times, "pick": best}
+        del a, b, r, cr
+        torch.cuda.empty_cache()
+    return picks, record
+
+
+def tune_plain_crossover(ctx, stream, dev) -> tuple[int, dict]:
+    import torch
+
+    sizes = [64, 96, 128, 160, 192, 256, 320, 384, 512, 640, 768, 1024]
+    record, ntt_faster = {}, {}
+    for m in sizes:
+        n = max(512, (64 << 20) // (8 * m))
+        a = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        b = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        r = torch.empty(2 * n * m, dtype=torch.int64, device=dev)
+        sp = stream.cuda_stream
+        t_cls = _timer(lambda: ctx.mul_full(a, b, r, n, m, stream=sp), 5, 2, stream)
+        t_ntt = _timer(lambda: ctx.mul_ntt(a, b, r, n, m, stream=sp), 5, 2, stream)
+        record[str(m)] = {"instances": n, "classical_ns_per_product": t_cls * 1e6 / n,
+                          "ntt_ns_per_product": t_ntt * 1e6 / n}
+        ntt_faster[m] = t_ntt < t_cls
+        del a, b, r
+        torch.cuda.empty_cache()
+    pick = 1025
+    for i, m in enumerate(sizes):
+        if all(ntt_faster[x] for x in sizes[i:]):
+            pick = m
+            break
+    return pick, record
+
+
+def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
+    import torch
+
+    import midint
+    import workloads
+
+    ops, pool, out_limbs = workloads.ragged_ops(n_ops=n_ops, seed=workloads.SEED_BASE + 3)
+    d_ops = torch.from_numpy(ops.view(np.uint8).copy()).to(dev)
+    d_in = torch.from_numpy(pool.view(np.int64)).to(dev)
+    d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+    d_c = torch.empty(n_ops, dtype=torch.uint8, device=dev)
+    sb = midint.ragged_scratch_bytes(n_ops)
+    scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+    sp = stream.cuda_stream
+    record = {}
+    ref = None
+    for th in (16, 24, 32, 48, 64, 80, 96, 112, 128, 129):
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, th)
+        ms = _timer(lambda: ctx.ragged_run(d_ops, n_ops, d_in, d_out, scr, sb, carry=d_c, stream=sp), 5, 2, stream)
+        out = d_out.cpu().numpy()
+        if ref is None:
+            ref = out.copy()
+        elif not np.array_equal(out, ref):
+            raise SystemExit(f"autotune: ragged results differ at threshold {th}")
+        record[str(th)] = {"ms": ms}
+    pick = int(min(record, key=lambda k: record[k]["ms"]))
+    del d_ops, d_in, d_out, d_c, scr
+    torch.cuda.empty_cache()
+    return pick, {"ops": n_ops, "candidates": record}
+
+
+HEADER = """// tuning_table.h -- defaults of the tunable launch choices, written by
+// midint-arithmetic_gb300/autotune.py from measurements on {device} ({date}; the
+// record of the run is midint-arithmetic_gb300/tuning.json).  Hand edits are
+// overwritten by the next tuning run.
+#pragma once
+
+#include <cstdint>
+
+namespace mi {{
+namespace tuned {{
+
+// mi_mul_u64: square products of at least this many u64 limbs use the NTT.
+constexpr uint32_t kPlainNttMin = {plain};
+// Ragged runs: products whose shorter operand has at least this many u64
+// limbs use the NTT kernel (1..129).
+constexpr uint32_t kRaggedNttMin = {ragged};
+// Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
+// size class c = ceil(log2(u64 limbs)), c = 0..12.
+constexpr uint8_t kAddThreadBytes[13] = {{{add}}};
+
+}}  // namespace tuned
+}}  // namespace mi
+"""
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out-dir", default=".")
+    ap.add_argument("--apply", action="store_true", help="write into the package (csrc/, tuning.json)")
+    ap.add_argument("--ragged-ops", type=int, default=200000)
+    args = ap.parse_args()
+
+    import torch
+
+    import midint
+
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.Stream(dev)
+    ctx = midint.Context(0)
+    add_picks, add_rec = tune_add(ctx, stream, dev)
+    plain, plain_rec = tune_plain_crossover(ctx, stream, dev)
+    ragged, ragged_rec = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
+    ctx.close()
+    device = torch.cuda.get_device_name(0)
+    date = datetime.date.today().isoformat()
+    header = HEADER.format(device=device, date=date, plain=plain, ragged=ragged,
+                           add=", ".join(str(x) for x in add_picks))
+    record = {"device": device, "date": date, "torch": torch.__version__,
+              "picks": {"plain_ntt_min": plain, "ragged_ntt_min": ragged, "add_thread_bytes": add_picks},
+              "add": add_rec, "plain_crossover": plain_rec, "ragged_crossover": ragged_rec}
+    if args.apply:
+        hpath, jpath = os.path.join(HERE, "csrc", "tuning_table.h"), os.path.join(HERE, "tuning.json")
+    else:
+        os.makedirs(args.out_dir, exist_ok=True)
+        hpath, jpath = os.path.join(args.out_dir, "tuning_table.h"), os.path.join(args.out_dir, "tuning.json")
+    with open(hpath, "w") as f:
+        f.write(header)
+    with open(jpath, "w") as f:
+        json.dump(record, f, indent=1)
+    print(json.dumps(record["picks"]))
+
+
+if __name__ == "__main__":
+    main()

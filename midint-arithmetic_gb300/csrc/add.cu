@@ -213,58 +213,69 @@ mi_status launch_one(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, u
     return MI_OK;
 }
 
-// Picks (Q, GS) from the limb count; VEC needs 16-byte aligned rows.
+template <typename L, bool VEC, int OP, int Q>
+mi_status dispatch_gs(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, uint32_t gs,
+                      cudaStream_t st) {
+    switch (gs) {
+        case 1: return launch_one<L, Q, 1, VEC, OP>(a, b, r, carry, n, m, st);
+        case 2: return launch_one<L, Q, 2, VEC, OP>(a, b, r, carry, n, m, st);
+        case 4: return launch_one<L, Q, 4, VEC, OP>(a, b, r, carry, n, m, st);
+        case 8: return launch_one<L, Q, 8, VEC, OP>(a, b, r, carry, n, m, st);
+        case 16: return launch_one<L, Q, 16, VEC, OP>(a, b, r, carry, n, m, st);
+        case 32: return launch_one<L, Q, 32, VEC, OP>(a, b, r, carry, n, m, st);
+        case 64: return launch_one<L, Q, 64, VEC, OP>(a, b, r, carry, n, m, st);
+        case 128: return launch_one<L, Q, 128, VEC, OP>(a, b, r, carry, n, m, st);
+        case 256: return launch_one<L, Q, 256, VEC, OP>(a, b, r, carry, n, m, st);
+        case 512: return launch_one<L, Q, 512, VEC, OP>(a, b, r, carry, n, m, st);
+        case 1024: return launch_one<L, Q, 1024, VEC, OP>(a, b, r, carry, n, m, st);
+        default: return set_error(MI_EINVAL, "add: %u limbs exceeds the single-group maximum", m);
+    }
+}
+
+// Q = thread_bytes / sizeof(L) limbs per thread (16, 32 or 64 bytes, raised
+// until the group fits 1024 threads), GS = pow2ceil(m / Q) threads per
+// instance.  VEC needs 16-byte aligned rows.
 template <typename L, bool VEC, int OP>
-mi_status dispatch(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, cudaStream_t st) {
-    constexpr int QS = 16 / sizeof(L);   // limbs per 128-bit load: 2 (u64) or 4 (u32)
-    if (m <= uint32_t(QS * 32)) {
-        const uint32_t gs = pow2ceil((m + QS - 1) / QS);
-        switch (gs) {
-            case 1: return launch_one<L, QS, 1, VEC, OP>(a, b, r, carry, n, m, st);
-            case 2: return launch_one<L, QS, 2, VEC, OP>(a, b, r, carry, n, m, st);
-            case 4: return launch_one<L, QS, 4, VEC, OP>(a, b, r, carry, n, m, st);
-            case 8: return launch_one<L, QS, 8, VEC, OP>(a, b, r, carry, n, m, st);
-            case 16: return launch_one<L, QS, 16, VEC, OP>(a, b, r, carry, n, m, st);
-            default: return launch_one<L, QS, 32, VEC, OP>(a, b, r, carry, n, m, st);
-        }
-    }
-    constexpr int Q2 = 2 * QS;  // 32 bytes per thread for wide integers
-    if (m <= uint32_t(Q2 * 1024)) {
-        const uint32_t gs = pow2ceil((m + Q2 - 1) / Q2);
-        switch (gs) {
-            case 32: return launch_one<L, Q2, 32, VEC, OP>(a, b, r, carry, n, m, st);
-            case 64: return launch_one<L, Q2, 64, VEC, OP>(a, b, r, carry, n, m, st);
-            case 128: return launch_one<L, Q2, 128, VEC, OP>(a, b, r, carry, n, m, st);
-            case 256: return launch_one<L, Q2, 256, VEC, OP>(a, b, r, carry, n, m, st);
-            case 512: return launch_one<L, Q2, 512, VEC, OP>(a, b, r, carry, n, m, st);
-            default: return launch_one<L, Q2, 1024, VEC, OP>(a, b, r, carry, n, m, st);
-        }
-    }
-    return set_error(MI_EINVAL, "add: %u limbs exceeds the single-group maximum", m);
+mi_status dispatch(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, uint32_t thread_bytes,
+                   cudaStream_t st) {
+    constexpr uint32_t QS = 16 / sizeof(L);  // limbs per 128-bit access
+    uint32_t q = thread_bytes >= 64 ? 4 * QS : (thread_bytes >= 32 ? 2 * QS : QS);
+    while (q < 4 * QS && pow2ceil((m + q - 1) / q) > 1024) q *= 2;
+    const uint32_t gs = pow2ceil((m + q - 1) / q);
+    if (q == QS) return dispatch_gs<L, VEC, OP, QS>(a, b, r, carry, n, m, gs, st);
+    if (q == 2 * QS) return dispatch_gs<L, VEC, OP, 2 * QS>(a, b, r, carry, n, m, gs, st);
+    return dispatch_gs<L, VEC, OP, 4 * QS>(a, b, r, carry, n, m, gs, st);
 }
 
 }  // namespace
 
+uint32_t add_size_class(uint64_t bytes) {
+    const uint64_t limbs = (bytes + 7) / 8;
+    uint32_t c = 0;
+    while (c < 12 && (uint64_t(1) << c) < limbs) ++c;
+    return c;
+}
+
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, int op, cudaStream_t st) {
+                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st) {
     const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (limbs % 2 == 0);
     if (op == ADD_SIX) {
-        return vec ? dispatch<uint64_t, true, ADD_SIX>(a, b, r, nullptr, n, limbs, st)
-                   : dispatch<uint64_t, false, ADD_SIX>(a, b, r, nullptr, n, limbs, st);
+        return vec ? dispatch<uint64_t, true, ADD_SIX>(a, b, r, nullptr, n, limbs, thread_bytes, st)
+                   : dispatch<uint64_t, false, ADD_SIX>(a, b, r, nullptr, n, limbs, thread_bytes, st);
     }
-    return vec ? dispatch<uint64_t, true, ADD_PLAIN>(a, b, r, carry, n, limbs, st)
-               : dispatch<uint64_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, st);
+    return vec ? dispatch<uint64_t, true, ADD_PLAIN>(a, b, r, carry, n, limbs, thread_bytes, st)
+               : dispatch<uint64_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, thread_bytes, st);
 }
 
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, cudaStream_t st) {
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st) {
     // An even number of u32 limbs on 8-byte aligned rows is the same bytes as
     // half as many u64 limbs, with the same carry-out.
     if (limbs % 2 == 0 && aligned8(a) && aligned8(b) && aligned8(r))
         return launch_add_u64(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
-                              reinterpret_cast<uint64_t*>(r), carry, n, limbs / 2, ADD_PLAIN, st);
+                              reinterpret_cast<uint64_t*>(r), carry, n, limbs / 2, ADD_PLAIN, thread_bytes, st);
     // Odd limb counts (or 4-byte aligned rows) cannot use 128-bit accesses.
-    return dispatch<uint32_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, st);
+    return dispatch<uint32_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, thread_bytes, st);
 }
 
 }  // namespace mi

@@ -77,6 +77,11 @@ mi_status check_batch(const void* a, const void* b, const void* r, uint32_t limb
     return MI_OK;
 }
 
+// Operand bytes per thread of an addition from the context's tuning table.
+uint32_t add_bytes(mi_ctx ctx, uint32_t limbs, int limb_bytes) {
+    return ctx->add_thread_bytes[add_size_class(uint64_t(limbs) * uint32_t(limb_bytes))];
+}
+
 mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* carry, uint32_t n, uint32_t limbs,
                   mi_stream stream, int limb_bytes, int op) {
     const uint32_t maxl = kAddMaxLimbs64 * (8 / limb_bytes);
@@ -90,11 +95,12 @@ mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* ca
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
     cudaStream_t st = pick_stream(ctx, stream);
+    const uint32_t tb = add_bytes(ctx, limbs, limb_bytes);
     if (limb_bytes == 8)
         return launch_add_u64(static_cast<const uint64_t*>(a), static_cast<const uint64_t*>(b),
-                              static_cast<uint64_t*>(r), carry, n, limbs, op, st);
+                              static_cast<uint64_t*>(r), carry, n, limbs, op, tb, st);
     return launch_add_u32(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
-                          static_cast<uint32_t*>(r), carry, n, limbs, st);
+                          static_cast<uint32_t*>(r), carry, n, limbs, tb, st);
 }
 
 mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n, uint32_t limbs, mi_stream stream,
@@ -275,6 +281,41 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
     return MI_OK;
 }
 
+mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) {
+    if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
+    switch (knob) {
+        case MI_TUNE_PLAIN_NTT_MIN:
+            if (value < 1 || value > kNttMaxLimbs + 1)
+                return set_error(MI_EINVAL, "plain_ntt_min %u outside 1..%u", value, kNttMaxLimbs + 1);
+            ctx->plain_ntt_min = value;
+            return MI_OK;
+        case MI_TUNE_RAGGED_NTT_MIN:
+            if (value < 1 || value > 129) return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..129", value);
+            ctx->ragged_ntt_min = value;
+            return MI_OK;
+        case MI_TUNE_ADD_THREAD_BYTES:
+            if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
+            if (value != 16 && value != 32 && value != 64)
+                return set_error(MI_EINVAL, "addition bytes per thread %u not 16, 32 or 64", value);
+            ctx->add_thread_bytes[cls] = uint8_t(value);
+            return MI_OK;
+        default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
+    }
+}
+
+mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value) {
+    if (ctx == nullptr || value == nullptr) return set_error(MI_EINVAL, "null context or value");
+    switch (knob) {
+        case MI_TUNE_PLAIN_NTT_MIN: *value = ctx->plain_ntt_min; return MI_OK;
+        case MI_TUNE_RAGGED_NTT_MIN: *value = ctx->ragged_ntt_min; return MI_OK;
+        case MI_TUNE_ADD_THREAD_BYTES:
+            if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
+            *value = ctx->add_thread_bytes[cls];
+            return MI_OK;
+        default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
+    }
+}
+
 mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry_out, uint32_t n,
                      uint32_t limbs, mi_stream stream) {
     return add_any(ctx, a, b, r, carry_out, n, limbs, stream, 8, ADD_PLAIN);
@@ -350,9 +391,10 @@ mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 4;
     return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                         [m, tb = add_bytes(ctx, m, 4)](void* da, void* db, void* dr, uint8_t*, uint32_t cnt,
+                                                         cudaStream_t st) {
                              return launch_add_u32(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
-                                                   static_cast<uint32_t*>(dr), nullptr, cnt, m, st);
+                                                   static_cast<uint32_t*>(dr), nullptr, cnt, m, tb, st);
                          });
 }
 
@@ -486,9 +528,10 @@ mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, 
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
     const size_t row = size_t(limbs) * 8;
     return host_pipeline(ctx, h_a, h_b, h_r, h_carry, n, row, row,
-                         [limbs](void* da, void* db, void* dr, uint8_t* dc, uint32_t cnt, cudaStream_t st) {
+                         [limbs, tb = add_bytes(ctx, limbs, 8)](void* da, void* db, void* dr, uint8_t* dc,
+                                                                 uint32_t cnt, cudaStream_t st) {
                              return launch_add_u64(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
-                                                   static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, st);
+                                                   static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, tb, st);
                          });
 }
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "ntt_host.h"
+#include "tuning_table.h"
 
 struct mi_ctx_s {
     int device = 0;
@@ -19,9 +20,14 @@ struct mi_ctx_s {
     // ragged batches: products whose shorter operand has at least this many
     // u64 limbs go through the NTT kernel (at most 129: classical groups hold
     // 128 limbs of the shorter operand)
-    uint32_t ragged_ntt_min = 129;
+    uint32_t ragged_ntt_min = mi::tuned::kRaggedNttMin;
     // mi_mul_u64: square products of at least this many u64 limbs use the NTT
-    uint32_t plain_ntt_min = 256;
+    uint32_t plain_ntt_min = mi::tuned::kPlainNttMin;
+    // addition: operand bytes per thread by size class ceil(log2(u64 limbs))
+    uint8_t add_thread_bytes[13] = {};
+    mi_ctx_s() {
+        for (int c = 0; c < 13; ++c) add_thread_bytes[c] = mi::tuned::kAddThreadBytes[c];
+    }
 };
 
 struct mi_graph_s {

@@ -12,15 +12,22 @@ enum AddOp : int { ADD_PLAIN = 0, ADD_SIX = 1 };
 
 // Batched addition on u64 or u32 limbs (op = ADD_PLAIN or ADD_SIX).
 // Arguments are already validated; n > 0, limbs > 0.
+// thread_bytes: operand bytes each thread owns (16, 32 or 64; raised where the
+// instance would need a group of more than 1024 threads).
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, int op, cudaStream_t st);
+                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st);
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, cudaStream_t st);
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st);
+// Size class of an addition of `bytes` per operand: ceil(log2(u64 limbs)).
+uint32_t add_size_class(uint64_t bytes);
 
 // Classical multiplication on u32 limb views (a u64 buffer with m limbs is a
 // u32 buffer with 2m limbs).  full: r has 2*n32 limbs per instance, else n32.
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
                              bool full, cudaStream_t st);
+
+// Low n32 limbs of a*b per instance (u32 limb views), n32 > 8.
+mi_status launch_mul_lo(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st);
 
 // ((a^2 + b)(b^2 + b) + ab) mod 2^(32*n32) per instance (u32 limb views).
 mi_status launch_poly(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st);

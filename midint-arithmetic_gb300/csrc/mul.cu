@@ -5,7 +5,8 @@
 // instance is one square product of mul_core.cuh, computed by a group of
 // NT = pow2ceil(n32/8) threads; a block of max(256, NT) threads holds 256/NT
 // groups and strides over the batch.  `full` selects the 2*n32-limb product or
-// its low n32 limbs (the reference's semantics).
+// its low n32 limbs (the reference's semantics); low halves of more than one
+// block of limbs go to the half-work kernel of mul_lo.cu.
 #include <cstdio>
 
 #include "common.cuh"
@@ -28,7 +29,7 @@ struct MulShape {
 };
 
 template <int NT, bool VEC>
-__global__ void __launch_bounds__(NT > 256 ? NT : 256)
+__global__ void __launch_bounds__(NT > 256 ? NT : 256, NT == 2 ? 2 : 3)
     k_mul(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ r, uint32_t n,
           uint32_t n32, bool full) {
     using S = MulShape<NT>;
@@ -44,6 +45,7 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
     uint2* slots = reinterpret_cast<uint2*>(sT) + grp * NT * classic::PAIRS;
     uint32_t* scr = sA;  // only used after the tile loop, by groups wider than a warp
     const uint32_t rlen = full ? 2 * n32 : n32;
+    const uint32_t nb = (n32 + T - 1) / T;  // blocks holding limbs; the rest of the NT are zero padding
     const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
 
     // Every group of a block runs the same trip count (wide groups synchronise
@@ -56,189 +58,16 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256)
         classic::stage_b<NT, VEC>(gB4, b + off, n32, valid, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi);
+        if (nb == NT)  // no padding: the trip count is a compile-time constant
+            classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi, NT);
+        else
+            classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi, nb);
         if (valid) {
             uint32_t* rr = r + inst * rlen;
             classic::store_block<VEC>(rr, t * T, rlen, ulo);
             if (full) classic::store_block<VEC>(rr, (t + NT) * T, rlen, uhi);
         }
         group_sync<NT>();  // shared memory is reused by the next instance
-    }
-}
-
-// Shape of the low-half kernels: NH threads per instance, NB = 2*NH blocks per
-// operand.
-template <int NH>
-struct LoShape {
-    static constexpr int BLOCK = NH > 256 ? NH : 256;
-    static constexpr int IPB = BLOCK / NH;
-    static constexpr int NB = 2 * NH;
-    static constexpr int WPAD = NB * T;  // words per operand
-    static constexpr size_t SMEM = size_t(2 * IPB * WPAD + BLOCK * classic::PER_T) * 4;
-};
-
-// The low n32 limbs of a*b (the reference's bmulKerQ semantics) with half the
-// partial products of a full product: classic::low_product per instance.
-template <int NH, bool VEC>
-__global__ void __launch_bounds__(NH > 256 ? NH : 256)
-    k_mul_lo(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ r, uint32_t n,
-             uint32_t n32) {
-    using S = LoShape<NH>;
-    extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* sA = smem;
-    uint32_t* sB = sA + S::IPB * S::WPAD;
-    uint32_t* sT = sB + S::IPB * S::WPAD;
-    const uint32_t grp = threadIdx.x / NH;
-    const uint32_t t = threadIdx.x % NH;
-    uint4* gA4 = reinterpret_cast<uint4*>(sA + grp * S::WPAD);
-    uint4* gB4 = reinterpret_cast<uint4*>(sB + grp * S::WPAD);
-    uint2* slots = reinterpret_cast<uint2*>(sT) + grp * NH * classic::PAIRS;
-    uint32_t* scr = sA;  // only used after the tile loop, by groups wider than a warp
-    const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
-    for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride) {
-        const uint64_t inst = base + grp;
-        const bool valid = inst < n;
-        const uint64_t off = valid ? inst * n32 : 0;
-        classic::stage_planes<S::NB, NH, VEC>(gA4, a + off, n32, valid, t);
-        classic::stage_planes<S::NB, NH, VEC>(gB4, b + off, n32, valid, t);
-        group_sync<NH>();
-        uint32_t ulo[T], uhi[T];
-        classic::low_product<NH>(gA4, gB4, slots, scr, t, ulo, uhi);
-        if (valid) {
-            uint32_t* rr = r + inst * n32;
-            classic::store_block<VEC>(rr, t * T, n32, ulo);
-            classic::store_block<VEC>(rr, (NH + t) * T, n32, uhi);
-        }
-        group_sync<NH>();
-    }
-}
-
-// Block q (limbs qT..qT+T-1) of an n32-limb row, zero beyond n32.
-template <bool VEC>
-__device__ __forceinline__ void load_block(uint32_t (&x)[T], const uint32_t* __restrict__ row, uint32_t q,
-                                           uint32_t n32, bool valid) {
-    const uint32_t o = q * T;
-    if (VEC && valid && o + T <= n32) {
-#pragma unroll
-        for (int h = 0; h < T / 4; ++h) {
-            const uint4 v = __ldcs(reinterpret_cast<const uint4*>(row + o) + h);
-            x[4 * h] = v.x, x[4 * h + 1] = v.y, x[4 * h + 2] = v.z, x[4 * h + 3] = v.w;
-        }
-    } else {
-#pragma unroll
-        for (int w = 0; w < T; ++w) x[w] = (valid && o + w < n32) ? __ldcs(row + o + w) : 0u;
-    }
-}
-
-// A thread's two blocks (q and NH+q) of an operand held in registers.
-struct Pair {
-    uint32_t lo[T], hi[T];
-};
-
-// Zeroes the limbs at or beyond n32 (everything is mod 2^(32*n32)).
-template <int NH>
-__device__ __forceinline__ void mask_pair(Pair& x, uint32_t q, uint32_t n32) {
-#pragma unroll
-    for (int w = 0; w < T; ++w) {
-        if (q * T + w >= n32) x.lo[w] = 0;
-        if ((NH + q) * T + w >= n32) x.hi[w] = 0;
-    }
-}
-
-// Stages register operands x (as A) and y (as B) in the plane layout.
-template <int NH>
-__device__ __forceinline__ void stage_pair(uint4* g4, uint32_t q, const Pair& x) {
-    constexpr int NB = 2 * NH;
-    g4[q] = make_uint4(x.lo[0], x.lo[1], x.lo[2], x.lo[3]);
-    g4[NB + q] = make_uint4(x.lo[4], x.lo[5], x.lo[6], x.lo[7]);
-    g4[NH + q] = make_uint4(x.hi[0], x.hi[1], x.hi[2], x.hi[3]);
-    g4[NB + NH + q] = make_uint4(x.hi[4], x.hi[5], x.hi[6], x.hi[7]);
-}
-
-// (x + y) mod 2^(32*T*NB) over the group's blocks.
-template <int NH>
-__device__ __forceinline__ void add_pair(const Pair& x, const Pair& y, Pair& r, uint32_t* scr) {
-    bool g0, p0, g1, p1;
-    uint32_t c0, c1;
-    chunk_add<uint32_t, T>(x.lo, y.lo, r.lo, g0, p0);
-    chunk_add<uint32_t, T>(x.hi, y.hi, r.hi, g1, p1);
-    const uint32_t cl = group_carry<NH>(g0, p0, 0u, &c0, scr);
-    const uint32_t ch = group_carry<NH>(g1, p1, c0, &c1, scr);
-    chunk_inc<uint32_t, T>(r.lo, cl);
-    chunk_inc<uint32_t, T>(r.hi, ch);
-}
-
-// r = ((a^2 + b)(b^2 + b) + ab) mod 2^(32*n32): the composite of the
-// reference's polyKerQ (cuda/ker-classic-mul.cu.h:500-575) in one kernel, as
-// four low-half products.  The group keeps its blocks of a, b and the partial
-// results in registers and restages the operands of each product in shared
-// memory; ab is formed first so that a is dead after a^2.
-template <int NH, bool VEC>
-__global__ void __launch_bounds__(NH > 256 ? NH : 256, 2)
-    k_poly(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ r, uint32_t n,
-           uint32_t n32) {
-    using S = LoShape<NH>;
-    extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* sA = smem;
-    uint32_t* sB = sA + S::IPB * S::WPAD;
-    uint32_t* sT = sB + S::IPB * S::WPAD;
-    const uint32_t grp = threadIdx.x / NH;
-    const uint32_t t = threadIdx.x % NH;
-    uint4* gA4 = reinterpret_cast<uint4*>(sA + grp * S::WPAD);
-    uint4* gB4 = reinterpret_cast<uint4*>(sB + grp * S::WPAD);
-    uint2* slots = reinterpret_cast<uint2*>(sT) + grp * NH * classic::PAIRS;
-    // per-warp carry words of wide groups: the operand area, which is free
-    // whenever a carry is resolved (after a product's tile loop, and between a
-    // product and the next staging)
-    uint32_t* scr = sA;
-    const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
-    for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride) {
-        const uint64_t inst = base + grp;
-        const bool valid = inst < n;
-        Pair xa, xb, t6, u, v;
-        {
-            const uint32_t* ra = a + (valid ? inst * n32 : 0);
-            const uint32_t* rb = b + (valid ? inst * n32 : 0);
-            load_block<VEC>(xa.lo, ra, t, n32, valid);
-            load_block<VEC>(xa.hi, ra, NH + t, n32, valid);
-            load_block<VEC>(xb.lo, rb, t, n32, valid);
-            load_block<VEC>(xb.hi, rb, NH + t, n32, valid);
-        }
-        stage_pair<NH>(gA4, t, xa);  // t6 = a*b
-        stage_pair<NH>(gB4, t, xb);
-        group_sync<NH>();
-        classic::low_product<NH>(gA4, gB4, slots, scr, t, t6.lo, t6.hi);
-        mask_pair<NH>(t6, t, n32);
-        group_sync<NH>();
-        stage_pair<NH>(gA4, t, xa);  // t1 = a*a
-        stage_pair<NH>(gB4, t, xa);
-        group_sync<NH>();
-        classic::low_product<NH>(gA4, gB4, slots, scr, t, u.lo, u.hi);
-        mask_pair<NH>(u, t, n32);
-        group_sync<NH>();
-        add_pair<NH>(u, xb, xa, scr);  // t2 = t1 + b (into xa)
-        mask_pair<NH>(xa, t, n32);
-        stage_pair<NH>(gA4, t, xb);  // t3 = b*b
-        stage_pair<NH>(gB4, t, xb);
-        group_sync<NH>();
-        classic::low_product<NH>(gA4, gB4, slots, scr, t, u.lo, u.hi);
-        mask_pair<NH>(u, t, n32);
-        group_sync<NH>();
-        add_pair<NH>(u, xb, v, scr);  // t4 = t3 + b
-        mask_pair<NH>(v, t, n32);
-        stage_pair<NH>(gA4, t, xa);  // t5 = t2*t4
-        stage_pair<NH>(gB4, t, v);
-        group_sync<NH>();
-        classic::low_product<NH>(gA4, gB4, slots, scr, t, u.lo, u.hi);
-        mask_pair<NH>(u, t, n32);
-        group_sync<NH>();
-        add_pair<NH>(u, t6, v, scr);  // r = t5 + t6
-        if (valid) {
-            uint32_t* rr = r + inst * n32;
-            classic::store_block<VEC>(rr, t * T, n32, v.lo);
-            classic::store_block<VEC>(rr, (NH + t) * T, n32, v.hi);
-        }
-        group_sync<NH>();
     }
 }
 
@@ -280,59 +109,13 @@ mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n
     }
 }
 
-// Launches a low-half kernel (k_mul_lo or k_poly) with NH threads per instance.
-template <int NH, bool VEC, bool POLY>
-mi_status launch_lo_nh(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
-                       cudaStream_t st) {
-    using S = LoShape<NH>;
-    auto kern = POLY ? k_poly<NH, VEC> : k_mul_lo<NH, VEC>;
-    static bool attr_done[64] = {};
-    int dev = 0;
-    MI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-        attr_done[dev] = true;
-    }
-    uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
-    const uint64_t cap = uint64_t(sm_count()) * 32;
-    if (blocks > cap) blocks = cap;
-    kern<<<dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st>>>(a, b, r, n, n32);
-    MI_CUDA_TRY(cudaGetLastError());
-    return MI_OK;
-}
-
-// NB = 2*NH = pow2ceil(blocks of T limbs), at least 2.
-template <bool VEC, bool POLY>
-mi_status dispatch_lo(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
-                      cudaStream_t st) {
-    uint32_t nb = pow2ceil((n32 + T - 1) / T);
-    if (nb < 2) nb = 2;
-    switch (nb / 2) {
-        case 1: return launch_lo_nh<1, VEC, POLY>(a, b, r, n, n32, st);
-        case 2: return launch_lo_nh<2, VEC, POLY>(a, b, r, n, n32, st);
-        case 4: return launch_lo_nh<4, VEC, POLY>(a, b, r, n, n32, st);
-        case 8: return launch_lo_nh<8, VEC, POLY>(a, b, r, n, n32, st);
-        case 16: return launch_lo_nh<16, VEC, POLY>(a, b, r, n, n32, st);
-        case 32: return launch_lo_nh<32, VEC, POLY>(a, b, r, n, n32, st);
-        case 64: return launch_lo_nh<64, VEC, POLY>(a, b, r, n, n32, st);
-        case 128: return launch_lo_nh<128, VEC, POLY>(a, b, r, n, n32, st);
-        default: return set_error(MI_EINVAL, "%s: %u u32 limbs exceeds the classical maximum", POLY ? "poly" : "mul",
-                                  n32);
-    }
-}
-
 }  // namespace
-
-mi_status launch_poly(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st) {
-    const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (n32 % 4 == 0);
-    return vec ? dispatch_lo<true, true>(a, b, r, n, n32, st) : dispatch_lo<false, true>(a, b, r, n, n32, st);
-}
 
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
                              cudaStream_t st) {
     const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (n32 % 4 == 0);
     if (!full && n32 > T)  // low halves: half the partial products of a full product
-        return vec ? dispatch_lo<true, false>(a, b, r, n, n32, st) : dispatch_lo<false, false>(a, b, r, n, n32, st);
+        return launch_mul_lo(a, b, r, n, n32, st);
     return vec ? dispatch<true>(a, b, r, n, n32, full, st) : dispatch<false>(a, b, r, n, n32, full, st);
 }
 

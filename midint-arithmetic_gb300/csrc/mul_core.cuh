@@ -143,15 +143,18 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
     }
 }
 
-// The full product of the group's staged A (NT blocks) and B (NT blocks).
-// On return thread t holds output blocks t (lo, limbs tT..tT+T-1) and t+NT
-// (hi), fully carried.  `slots` is the group's PAIRS*NT 64-bit shared slots
+// The full product of the group's staged A (NT blocks) and B (NT blocks), of
+// which only the first nb hold nonzero limbs (1 <= nb <= NT).  Steps k >= nb
+// (A-block k zero for the whole group) are not run; anti-diagonal t is then
+// complete after step min(t, nb-1).  On return thread t holds output blocks t (lo,
+// limbs tT..tT+T-1) and t+NT (hi), fully carried.  `slots` is the group's PAIRS*NT 64-bit shared slots
 // (pair w of thread l at slots[w*NT + l]), `scr` per-warp scratch for groups
 // wider than a warp.  Starts and ends with the group's shared areas free for
 // reuse by the caller after a group_sync.
 template <int NT>
 __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
-                                               uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+                                               uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
+                                               uint32_t nb = NT) {
     auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NT + lane]; };
     DiagAcc s;
 #pragma unroll
@@ -160,8 +163,9 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
     for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
 #pragma unroll
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+    const uint32_t snap_k = t < nb ? t : nb - 1;
 #pragma unroll 2
-    for (uint32_t k = 0; k < uint32_t(NT); ++k) {
+    for (uint32_t k = 0; k < nb; ++k) {
         const uint32_t j = (t - k) & uint32_t(NT - 1);
         uint32_t A[T], B[T];
         const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * T)[0];
@@ -173,7 +177,7 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
         B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
         tile_mac(A, B, s);
-        if (k == t) {
+        if (k == snap_k) {
             // anti-diagonal t is complete: snapshot the accumulator, straight
             // from its register pairs
 #pragma unroll
@@ -296,17 +300,21 @@ __device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restri
 }
 
 // The low NB = 2*NH blocks of the product of A and B (NB blocks each, both in
-// the two-plane layout).  Only the anti-diagonals s < NB are needed; thread t
-// of a group of NH threads owns s = t (t+1 tiles) and its mirror
-// s = NB-1-t (NB-t tiles): NB+1 tiles for every thread, the reference's
+// the two-plane layout), of which only the first nb hold nonzero limbs
+// (1 <= nb <= NB).  Only the anti-diagonals s < nb reach the low nb blocks;
+// with H = ceil(nb/2), thread t < H owns s = t (t+1 tiles) and its mirror
+// s = nb-1-t (nb-t tiles): nb+1 tiles for every thread, the reference's
 // column pairing (cuda/ker-classic-mul.cu.h:406-423) at tile granularity.  In
 // the first t+1 steps thread t walks anti-diagonal t (A-block k broadcast,
-// B-block t-k); then its mirror (A-block k-t-1, B-block NB-k broadcast).  On
-// return thread t holds output blocks t (ulo) and NH+t (uhi), fully carried;
-// the carry out of block NB-1 is dropped (the product mod 2^(32*T*NB)).
+// B-block t-k); then its mirror (A-block k-t-1, B-block nb-k broadcast).
+// Threads without a mirror (t >= H, and t = (nb-1)/2 for odd nb) read the
+// zero block nb instead, which exists whenever they do.  On return thread t
+// holds output blocks t (ulo) and NH+t (uhi), fully carried; the carry out of
+// block NB-1 is dropped (the product mod 2^(32*T*NB)).
 template <int NH>
 __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
-                                            uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T]) {
+                                            uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
+                                            uint32_t nb = 2 * NH) {
     constexpr uint32_t NB = 2 * NH;
     auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NH + lane]; };
     DiagAcc s;
@@ -316,11 +324,14 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
     for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
 #pragma unroll
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+    const uint32_t H = (nb + 1) / 2;
+    const bool mirror = t < H && t < nb - 1 - t;  // owns a second anti-diagonal
 #pragma unroll 2
-    for (uint32_t k = 0; k <= NB; ++k) {
+    for (uint32_t k = 0; k <= nb; ++k) {
         const bool first = k <= t;
-        const uint32_t i = first ? k : k - t - 1;
-        const uint32_t j = first ? t - k : NB - k;
+        uint32_t i = first ? k : k - t - 1;
+        const uint32_t j = first ? t - k : nb - k;
+        if (first ? t >= H : !mirror) i = nb;  // a zero block
         uint32_t A[T], B[T];
         const uint4 a0 = gA4[i];
         const uint4 a1 = gA4[NB + i];
@@ -342,7 +353,7 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
         }
     }
 
-    // D1 = anti-diagonal t (the snapshot), D2 = anti-diagonal NB-1-t
+    // D1 = anti-diagonal t (the snapshot), D2 = anti-diagonal nb-1-t
     {
         uint32_t d1[ACC], d2[ACC];
         uint32_t snap[2 * PAIRS];
@@ -368,11 +379,12 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
     }
     group_sync<NH>();
 
-    // word w of anti-diagonal value D_s (s < NB): thread s holds it as D1 for
-    // s < NH, thread NB-1-s as D2 otherwise
+    // word w of anti-diagonal value D_s: thread s holds it as D1 for s < H,
+    // thread nb-1-s as D2 for H <= s < nb; beyond nb it is not needed (zero)
     auto diag = [&](uint32_t sd, int w) -> uint32_t {
-        const bool low = sd < NH;
-        const uint2 v = slot((low ? 0 : 9) + w / 2, low ? sd : NB - 1 - sd);
+        if (sd >= nb) return 0u;
+        const bool low = sd < H;
+        const uint2 v = slot((low ? 0 : 9) + w / 2, low ? sd : nb - 1 - sd);
         return (w & 1) ? v.y : v.x;
     };
     // output block q: L_q + H_(q-1) + O_(q-2)

@@ -33,6 +33,7 @@ RAGGED_NOALLOC_MAX_OPS = 65536
 # Every symbol include/midint.h declares, with (restype, argtypes).
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
 _S = ctypes.c_int  # mi_status
+TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES = 0, 1, 2
 SIGNATURES = {
     "mi_version": (_I, []),
     "mi_status_string": (ctypes.c_char_p, [_I]),
@@ -42,6 +43,8 @@ SIGNATURES = {
     "mi_ctx_synchronize": (_S, [_P]),
     "mi_ctx_stream": (_P, [_P]),
     "mi_ctx_set_crossover": (_S, [_P, _U32, _U32]),
+    "mi_ctx_set_tuning": (_S, [_P, _I, _U32, _U32]),
+    "mi_ctx_get_tuning": (_S, [_P, _I, _U32, _P]),
     "mi_add_u64": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add_u32": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add6_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
@@ -157,6 +160,15 @@ class Context:
 
     def set_crossover(self, ragged_ntt_min: int, plain_ntt_min: int) -> None:
         check(load().mi_ctx_set_crossover(self.handle, ragged_ntt_min, plain_ntt_min))
+
+    def set_tuning(self, knob: int, cls: int, value: int) -> None:
+        """Overrides one entry of the context's tuning table (TUNE_* knobs)."""
+        check(load().mi_ctx_set_tuning(self.handle, knob, cls, value))
+
+    def get_tuning(self, knob: int, cls: int = 0) -> int:
+        v = ctypes.c_uint32()
+        check(load().mi_ctx_get_tuning(self.handle, knob, cls, ctypes.byref(v)))
+        return v.value
 
     def close(self) -> None:
         if self.handle:

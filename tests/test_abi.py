@@ -51,6 +51,8 @@ def test_argument_errors_need_no_device(lib):
     assert lib.mi_compat_gpuAdd_u64(-1, 4, p, p, p) == midint.MI_EINVAL
     # a partial overlap of result and operand is refused; exact aliasing is allowed
     assert lib.mi_add_u64(None, p, p, p + 8, None, 2, 4, None) == midint.MI_EINVAL
+    assert lib.mi_ctx_set_tuning(None, midint.TUNE_ADD_THREAD_BYTES, 0, 16) == midint.MI_EINVAL
+    assert lib.mi_ctx_get_tuning(None, midint.TUNE_PLAIN_NTT_MIN, 0, p) == midint.MI_EINVAL
 
 
 def test_empty_batch_is_a_no_op(lib):

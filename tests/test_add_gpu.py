@@ -136,3 +136,45 @@ def test_host_add_with_carry(ctx):
     ctx.host_add(a, b, r, c, 1000, 64)
     wr, wc = O.add(a, b, 64)
     assert np.array_equal(r, wr) and np.array_equal(c, wc)
+
+
+@pytest.mark.parametrize("tb", [16, 32, 64])
+@pytest.mark.parametrize("m", [1, 2, 3, 8, 17, 64, 65, 200, 1024, 2049, 4096])
+def test_add_every_thread_width(lib, devmem, tb, m):
+    """Every bytes-per-thread choice of the tuning table gives the same sums."""
+    c = midint.Context(0)
+    try:
+        for cls in range(13):
+            c.set_tuning(midint.TUNE_ADD_THREAD_BYTES, cls, tb)
+        a, b = carry_stress(19, m, seed=5 * m + tb)
+        ra, ca = O.add(a, b, m)
+        r, cc = gpu_add(c, devmem, a, b, m)
+        assert np.array_equal(r, ra) and np.array_equal(cc, ca)
+        r6 = devmem.empty_words(a.view(np.uint32).size)
+        ba, pa = devmem.put(a)
+        bb, pb = devmem.put(b)
+        c.add6(pa, pb, r6[1], 19, m, stream=_stream())
+        torch.cuda.synchronize()
+        assert np.array_equal(devmem.get(r6[0], a.view(np.uint32).size), O.add6(a, b, m))
+        if m % 2 == 1:  # odd u32 limb counts take the scalar u32 kernel
+            a32, b32 = a.view(np.uint32)[: 19 * m], b.view(np.uint32)[: 19 * m]
+            r32, c32 = gpu_add(c, devmem, a32, b32, m, limb_bits=32)
+            ref32, cref32 = O.add(a32, b32, m)
+            assert np.array_equal(r32, ref32) and np.array_equal(c32, cref32)
+    finally:
+        c.close()
+
+
+def test_tuning_rejects_bad_values(ctx):
+    with pytest.raises(midint.MidintError):
+        ctx.set_tuning(midint.TUNE_ADD_THREAD_BYTES, 13, 16)
+    with pytest.raises(midint.MidintError):
+        ctx.set_tuning(midint.TUNE_ADD_THREAD_BYTES, 3, 24)
+    with pytest.raises(midint.MidintError):
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, 130)
+    with pytest.raises(midint.MidintError):
+        ctx.set_tuning(7, 0, 1)
+    old = ctx.get_tuning(midint.TUNE_PLAIN_NTT_MIN)
+    ctx.set_tuning(midint.TUNE_PLAIN_NTT_MIN, 0, 1025)
+    assert ctx.get_tuning(midint.TUNE_PLAIN_NTT_MIN) == 1025
+    ctx.set_tuning(midint.TUNE_PLAIN_NTT_MIN, 0, old)
