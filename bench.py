@@ -8,8 +8,10 @@ A step is one batched multiplication over the whole batch.
           operand sets whose total (4 x 64 MiB) exceeds the 129 MB L2, timed
           with CUDA events on the launching stream.
   e2e   : the same metric through the C ABI's host-buffer call
-          (mi_host_mul_full_u64) from pinned host memory, copies inside the
-          timed region.
+          (mi_host_mul_full_u64) from pinned host memory to pinned host
+          memory, every byte crossing the host link inside the timed region
+          (the tuned path: zero-copy kernels for multiplications; the copy
+          pipeline's time is reported beside it).
   roofline: the multiplication kernel against the integer-multiply ceiling
           measured in-process (mi_calib_mul32_peak), in 32x32-bit partial
           products/s; 65536 partial products per instance.
@@ -293,15 +295,29 @@ def run_ours(args):
         ctx.host_mul_full(han, hbn, hrn, N_MUL, M_MUL)
     barrier(world)
     e2e_steps = max(3, min(args.steps, 20))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx.host_mul_full(han, hbn, hrn, N_MUL, M_MUL)
-    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / e2e_steps)
-    if not np.array_equal(hrn.view(np.uint64)[: CHECK_N * 2 * M_MUL], got):
-        raise SystemExit("bench: e2e product differs from the device-resident one")
+
+    def host_steps() -> float:
+        hrn[:] = 0
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx.host_mul_full(han, hbn, hrn, N_MUL, M_MUL)
+        dt = (time.perf_counter() - t0) / e2e_steps
+        if not np.array_equal(hrn.view(np.uint64)[: CHECK_N * 2 * M_MUL], got):
+            raise SystemExit("bench: e2e product differs from the device-resident one")
+        return dt
+
+    zero_copy = ctx.get_tuning(midint.TUNE_HOST_ZERO_COPY, 1)
+    e2e_s = max_over_ranks(world, host_steps())
+    # the copy pipeline alone, for reference (the tuned default is above)
+    ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 0)
+    copy_s = max_over_ranks(world, host_steps())
+    ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, zero_copy)
+    path = ("mi_host_mul_full_u64 on pinned host buffers; the kernel reads the operands and writes the products "
+            "in place over the host link (zero-copy, the tuned choice for multiplications)" if zero_copy else
+            "mi_host_mul_full_u64 on pinned host buffers; chunked copy-in / compute / copy-out pipeline")
     e2e = {"value": world * N_MUL / e2e_s, "unit": "products/s", "h2d_bytes_per_step": 2 * in_bytes,
-           "d2h_bytes_per_step": 2 * in_bytes, "ms_per_step": e2e_s * 1e3,
-           "path": "mi_host_mul_full_u64 (pinned host buffers, 2-stream chunked copy/compute overlap)"}
+           "d2h_bytes_per_step": 2 * in_bytes, "ms_per_step": e2e_s * 1e3, "path": path,
+           "copy_pipeline_ms_per_step": copy_s * 1e3}
     del da, db, dr
     torch.cuda.empty_cache()
 

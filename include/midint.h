@@ -91,8 +91,21 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
  *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..129 (as ragged_ntt_min)
  *   MI_TUNE_ADD_THREAD_BYTES cls = ceil(log2(u64 limbs)) 0..12 of the
  *                            operands; value = bytes of each operand one
- *                            thread owns: 16, 32 or 64 */
-enum { MI_TUNE_PLAIN_NTT_MIN = 0, MI_TUNE_RAGGED_NTT_MIN = 1, MI_TUNE_ADD_THREAD_BYTES = 2 };
+ *                            thread owns: 16, 32 or 64
+ *   MI_TUNE_HOST_CHUNKS      cls = 0 additions, 1 multiplications; value
+ *                            1..64: chunks a host-buffer batch is cut into
+ *                            for copy/compute overlap
+ *   MI_TUNE_HOST_ZERO_COPY   cls as above; value 0 or 1: host-buffer calls
+ *                            whose buffers are all mapped pinned memory run
+ *                            the kernel on them in place (the buffers must
+ *                            hold the whole batch, as for the copies) */
+enum {
+    MI_TUNE_PLAIN_NTT_MIN = 0,
+    MI_TUNE_RAGGED_NTT_MIN = 1,
+    MI_TUNE_ADD_THREAD_BYTES = 2,
+    MI_TUNE_HOST_CHUNKS = 3,
+    MI_TUNE_HOST_ZERO_COPY = 4
+};
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
 mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value);
 

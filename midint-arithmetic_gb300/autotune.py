@@ -15,7 +15,9 @@ Knobs:
     size from which the NTT is faster at every larger measured size;
   * ragged classical/NTT crossover: the 200000-op mixed ragged workload (40%
     adds, operand bits log-uniform in [256, 65536]) timed end to end for every
-    candidate threshold; the fastest wins.
+    candidate threshold; the fastest wins;
+  * host-buffer calls: chunk count of the copy/compute pipeline, or zero-copy
+    kernels on mapped pinned buffers, timed on the multiplication batch.
 
 Usage:  python midint-arithmetic_gb300/autotune.py [--out-dir DIR] [--apply]
 (--apply writes into the package; otherwise into DIR, default the working
@@ -149,6 +151,50 @@ def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
     return pick, {"ops": n_ops, "candidates": record}
 
 
+def tune_host(ctx) -> tuple[list[int], list[int], dict]:
+    """Host-buffer calls on pinned buffers, wall-clock per call, for every chunk
+    count and with zero-copy: class 0 on the addition batch (65536 x 64 u64
+    limbs, with carries), class 1 on the classical multiplication batch (16384
+    x 128 u64 limbs, full products).  Each class takes its fastest choice."""
+    import time
+
+    import torch
+
+    import midint
+
+    def pinned(nwords):
+        return torch.randint(-2**62, 2**62, (nwords,), dtype=torch.int64).pin_memory()
+
+    nm, mm, na, ma = 16384, 128, 65536, 64
+    ha, hb, hr = pinned(nm * mm), pinned(nm * mm), pinned(2 * nm * mm)
+    aa, ab, ar = pinned(na * ma), pinned(na * ma), pinned(na * ma)
+    ac = torch.empty(na, dtype=torch.uint8).pin_memory()
+    calls = {0: lambda: ctx.host_add(aa, ab, ar, ac, na, ma), 1: lambda: ctx.host_mul_full(ha, hb, hr, nm, mm)}
+
+    def wall(fn, reps=20):
+        for _ in range(3):
+            fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    record, chunks, zero_copy = {}, [], []
+    for cls, name in ((0, "add"), (1, "mul")):
+        cands = {}
+        for zc, ch in [(0, c) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1)]:
+            ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
+            ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
+            cands[f"zero_copy={zc},chunks={ch}"] = {"zero_copy": zc, "chunks": ch, "ms": wall(calls[cls])}
+        best = min(cands.values(), key=lambda v: v["ms"])
+        ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, best["zero_copy"])
+        ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, best["chunks"])
+        chunks.append(best["chunks"])
+        zero_copy.append(best["zero_copy"])
+        record[name] = {"candidates": cands, "pick": best}
+    return chunks, zero_copy, record
+
+
 HEADER = """// tuning_table.h -- defaults of the tunable launch choices, written by
 // midint-arithmetic_gb300/autotune.py from measurements on {device} ({date}; the
 // record of the run is midint-arithmetic_gb300/tuning.json).  Hand edits are
@@ -168,6 +214,11 @@ constexpr uint32_t kRaggedNttMin = {ragged};
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {{{add}}};
+// Host-buffer calls, by operation class {{additions, multiplications}}: chunks a
+// large batch is cut into for copy/compute overlap, and whether kernels read
+// mapped pinned host buffers in place (1) instead.
+constexpr uint32_t kHostChunks[2] = {{{chunks}}};
+constexpr uint32_t kHostZeroCopy[2] = {{{zero_copy}}};
 
 }}  // namespace tuned
 }}  // namespace mi
@@ -179,6 +230,7 @@ def main():
     ap.add_argument("--out-dir", default=".")
     ap.add_argument("--apply", action="store_true", help="write into the package (csrc/, tuning.json)")
     ap.add_argument("--ragged-ops", type=int, default=200000)
+    ap.add_argument("--only", default="add,plain,ragged,host", help="knob groups to measure (others keep the table)")
     args = ap.parse_args()
 
     import torch
@@ -188,17 +240,31 @@ def main():
     dev = torch.device("cuda:0")
     stream = torch.cuda.Stream(dev)
     ctx = midint.Context(0)
-    add_picks, add_rec = tune_add(ctx, stream, dev)
-    plain, plain_rec = tune_plain_crossover(ctx, stream, dev)
-    ragged, ragged_rec = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
+    only = set(args.only.split(","))
+    # groups not measured keep the committed record
+    with open(os.path.join(HERE, "tuning.json")) as f:
+        old = json.load(f)
+    picks = dict(old["picks"])
+    picks.setdefault("host_chunks", [4, 6])
+    picks.setdefault("host_zero_copy", [0, 1])
+    record = {k: old.get(k) for k in ("add", "plain_crossover", "ragged_crossover", "host")}
+    if "add" in only:
+        picks["add_thread_bytes"], record["add"] = tune_add(ctx, stream, dev)
+    if "plain" in only:
+        picks["plain_ntt_min"], record["plain_crossover"] = tune_plain_crossover(ctx, stream, dev)
+    if "ragged" in only:
+        picks["ragged_ntt_min"], record["ragged_crossover"] = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
+    if "host" in only:
+        picks["host_chunks"], picks["host_zero_copy"], record["host"] = tune_host(ctx)
     ctx.close()
     device = torch.cuda.get_device_name(0)
     date = datetime.date.today().isoformat()
-    header = HEADER.format(device=device, date=date, plain=plain, ragged=ragged,
-                           add=", ".join(str(x) for x in add_picks))
-    record = {"device": device, "date": date, "torch": torch.__version__,
-              "picks": {"plain_ntt_min": plain, "ragged_ntt_min": ragged, "add_thread_bytes": add_picks},
-              "add": add_rec, "plain_crossover": plain_rec, "ragged_crossover": ragged_rec}
+    header = HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], ragged=picks["ragged_ntt_min"],
+                           chunks=", ".join(str(x) for x in picks["host_chunks"]),
+                           zero_copy=", ".join(str(x) for x in picks["host_zero_copy"]),
+                           add=", ".join(str(x) for x in picks["add_thread_bytes"]))
+    record = {"device": device, "date": date, "torch": torch.__version__, "measured": sorted(only),
+              "picks": picks, **record}
     if args.apply:
         hpath, jpath = os.path.join(HERE, "csrc", "tuning_table.h"), os.path.join(HERE, "tuning.json")
     else:

@@ -146,56 +146,89 @@ mi_status default_ctx(mi_ctx* out) {
 
 mi_status ensure_stage(mi_ctx ctx, size_t bytes) {
     if (bytes <= ctx->stage_cap) return MI_OK;
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < mi_ctx_s::kSlots; ++i) {
         if (ctx->stage[i]) cudaFree(ctx->stage[i]);
         ctx->stage[i] = nullptr;
     }
     ctx->stage_cap = 0;
     size_t cap = 1;
     while (cap < bytes) cap <<= 1;
-    for (int i = 0; i < 2; ++i) MI_CUDA_TRY(cudaMalloc(&ctx->stage[i], cap));
+    for (int i = 0; i < mi_ctx_s::kSlots; ++i) MI_CUDA_TRY(cudaMalloc(&ctx->stage[i], cap));
     ctx->stage_cap = cap;
     return MI_OK;
 }
 
-// Copies a batch through the device in chunks on two streams: while chunk c
-// computes and copies back on one stream, chunk c+1 copies in on the other.
-// `launch(da, db, dr, dcarry, count, stream)` runs the kernel on one chunk.
+// The device address of a mapped pinned host buffer, or null.
+void* mapped_host(const void* p) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
+// Runs `launch(da, db, dr, dcarry, count, stream)` over a batch of host
+// buffers, with the tuning of operation class `cls`.  With zero-copy enabled
+// for the class and every buffer mapped pinned memory, one
+// launch reads and writes them in place.  Otherwise the batch is cut into
+// chunks that cycle through kSlots device staging slots: chunk c copies in on
+// the copy-in stream (after the slot's previous copy-out), computes on compute
+// stream c % 2 and copies out on the copy-out stream, so copies in both
+// directions and the kernels of neighbouring chunks overlap.
+enum { HOST_ADD = 0, HOST_MUL = 1 };  // operation classes of the host tuning knobs
+
 template <typename F>
-mi_status host_pipeline(mi_ctx ctx, const void* h_a, const void* h_b, void* h_r, uint8_t* h_carry, uint32_t n,
-                        size_t in_row, size_t out_row, F launch) {
+mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, void* h_r, uint8_t* h_carry,
+                        uint32_t n, size_t in_row, size_t out_row, F launch) {
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
     std::lock_guard<std::mutex> lk(ctx->mu);
-    // Chunk so that each stream's staging area is at most 64 MiB and there are
-    // at least 4 chunks when the batch is big enough to gain from overlap.
-    const size_t per_inst = 2 * in_row + out_row + (h_carry ? 1 : 0) + 64;
-    uint64_t chunk = (64ull << 20) / per_inst;
+    if (ctx->host_zero_copy[cls]) {
+        void* da = mapped_host(h_a);
+        void* db = mapped_host(h_b);
+        void* dr = mapped_host(h_r);
+        void* dc = h_carry ? mapped_host(h_carry) : nullptr;
+        if (da && db && dr && (dc || !h_carry)) {
+            MI_TRY(launch(da, db, dr, static_cast<uint8_t*>(dc), n, ctx->pipe[2]));
+            MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[2]));
+            return MI_OK;
+        }
+    }
+    const size_t per_inst = 2 * in_row + out_row + (h_carry ? 1 : 0);
+    uint64_t chunk = (uint64_t(n) + ctx->host_chunks[cls] - 1) / ctx->host_chunks[cls];
+    const uint64_t max_chunk = (64ull << 20) / per_inst;  // at most 64 MiB per slot
+    if (chunk > max_chunk) chunk = max_chunk;
     if (chunk == 0) chunk = 1;
-    if (n >= 64 && chunk > (n + 3) / 4) chunk = (n + 3) / 4;
-    if (chunk > n) chunk = n;
     const size_t off_b = ((chunk * in_row + 255) / 256) * 256;
     const size_t off_r = off_b + ((chunk * in_row + 255) / 256) * 256;
     const size_t off_c = off_r + ((chunk * out_row + 255) / 256) * 256;
     MI_TRY(ensure_stage(ctx, off_c + chunk + 256));
+    cudaStream_t cin = ctx->pipe[0], cout = ctx->pipe[1];
     int c = 0;
     for (uint64_t base = 0; base < n; base += chunk, ++c) {
         const uint32_t cnt = uint32_t((n - base) < chunk ? (n - base) : chunk);
-        cudaStream_t st = ctx->pipe[c & 1];
-        char* stg = static_cast<char*>(ctx->stage[c & 1]);
+        const int slot = c % mi_ctx_s::kSlots;
+        cudaStream_t comp = ctx->pipe[2 + (c & 1)];
+        char* stg = static_cast<char*>(ctx->stage[slot]);
+        if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
         MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
-                                    cudaMemcpyHostToDevice, st));
+                                    cudaMemcpyHostToDevice, cin));
         MI_CUDA_TRY(cudaMemcpyAsync(stg + off_b, static_cast<const char*>(h_b) + base * in_row, cnt * in_row,
-                                    cudaMemcpyHostToDevice, st));
+                                    cudaMemcpyHostToDevice, cin));
+        MI_CUDA_TRY(cudaEventRecord(ctx->ev_in[slot], cin));
+        MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_in[slot], 0));
         MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt,
-                      st));
+                      comp));
+        MI_CUDA_TRY(cudaEventRecord(ctx->ev_k[slot], comp));
+        MI_CUDA_TRY(cudaStreamWaitEvent(cout, ctx->ev_k[slot], 0));
         MI_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_r) + base * out_row, stg + off_r, cnt * out_row,
-                                    cudaMemcpyDeviceToHost, st));
+                                    cudaMemcpyDeviceToHost, cout));
         if (h_carry)
-            MI_CUDA_TRY(cudaMemcpyAsync(h_carry + base, stg + off_c, cnt, cudaMemcpyDeviceToHost, st));
+            MI_CUDA_TRY(cudaMemcpyAsync(h_carry + base, stg + off_c, cnt, cudaMemcpyDeviceToHost, cout));
+        MI_CUDA_TRY(cudaEventRecord(ctx->ev_out[slot], cout));
     }
-    MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[0]));
-    MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[1]));
+    MI_CUDA_TRY(cudaStreamSynchronize(cout));
     return MI_OK;
 }
 
@@ -232,10 +265,16 @@ mi_status mi_ctx_create(int device, mi_ctx* out) {
     if (ctx == nullptr) return set_error(MI_ENOMEM, "mi_ctx_create: host allocation");
     ctx->device = device;
     mi_status st = MI_OK;
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->pipe[0], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->pipe[1], cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         st = set_error(MI_ECUDA, "mi_ctx_create: stream creation failed");
+    for (int i = 0; i < 4 && st == MI_OK; ++i)
+        if (cudaStreamCreateWithFlags(&ctx->pipe[i], cudaStreamNonBlocking) != cudaSuccess)
+            st = set_error(MI_ECUDA, "mi_ctx_create: stream creation failed");
+    for (int i = 0; i < mi_ctx_s::kSlots && st == MI_OK; ++i)
+        if (cudaEventCreateWithFlags(&ctx->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_k[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_out[i], cudaEventDisableTiming) != cudaSuccess)
+            st = set_error(MI_ECUDA, "mi_ctx_create: event creation failed");
     if (st == MI_OK) st = ntt_tables_create(&ctx->ntt);
     if (st != MI_OK) {
         mi_ctx_destroy(ctx);
@@ -249,12 +288,17 @@ mi_status mi_ctx_destroy(mi_ctx ctx) {
     if (ctx == nullptr) return MI_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 4; ++i) {
         if (ctx->pipe[i]) {
             cudaStreamSynchronize(ctx->pipe[i]);
             cudaStreamDestroy(ctx->pipe[i]);
         }
+    }
+    for (int i = 0; i < mi_ctx_s::kSlots; ++i) {
         if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+        if (ctx->ev_in[i]) cudaEventDestroy(ctx->ev_in[i]);
+        if (ctx->ev_k[i]) cudaEventDestroy(ctx->ev_k[i]);
+        if (ctx->ev_out[i]) cudaEventDestroy(ctx->ev_out[i]);
     }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     ntt_tables_destroy(&ctx->ntt);
@@ -299,6 +343,16 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
                 return set_error(MI_EINVAL, "addition bytes per thread %u not 16, 32 or 64", value);
             ctx->add_thread_bytes[cls] = uint8_t(value);
             return MI_OK;
+        case MI_TUNE_HOST_CHUNKS:
+            if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
+            if (value < 1 || value > 64) return set_error(MI_EINVAL, "host chunks %u outside 1..64", value);
+            ctx->host_chunks[cls] = value;
+            return MI_OK;
+        case MI_TUNE_HOST_ZERO_COPY:
+            if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
+            if (value > 1) return set_error(MI_EINVAL, "host zero-copy %u not 0 or 1", value);
+            ctx->host_zero_copy[cls] = value;
+            return MI_OK;
         default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
     }
 }
@@ -311,6 +365,11 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
         case MI_TUNE_ADD_THREAD_BYTES:
             if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
             *value = ctx->add_thread_bytes[cls];
+            return MI_OK;
+        case MI_TUNE_HOST_CHUNKS:
+        case MI_TUNE_HOST_ZERO_COPY:
+            if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
+            *value = knob == MI_TUNE_HOST_CHUNKS ? ctx->host_chunks[cls] : ctx->host_zero_copy[cls];
             return MI_OK;
         default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
     }
@@ -390,7 +449,7 @@ mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 4;
-    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+    return host_pipeline(ctx, HOST_ADD, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [m, tb = add_bytes(ctx, m, 4)](void* da, void* db, void* dr, uint8_t*, uint32_t cnt,
                                                          cudaStream_t st) {
                              return launch_add_u32(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
@@ -405,7 +464,7 @@ mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 8;
-    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+    return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                        static_cast<uint32_t*>(dr), cnt, 2 * m, false, st);
@@ -419,7 +478,7 @@ mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 4;
-    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+    return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                        static_cast<uint32_t*>(dr), cnt, m, false, st);
@@ -438,7 +497,7 @@ mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t*
     const uint32_t m = M / 4;  // u64 limbs
     const size_t row = size_t(m) * 8;
     // the NTT kernel, storing the low M digits (m limbs) of each product
-    return host_pipeline(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+    return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [ctx, m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
                              return launch_mul_ntt(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
                                                    static_cast<uint64_t*>(dr), cnt, m, ctx->ntt.params, st, true);
@@ -527,7 +586,7 @@ mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, 
     MI_TRY(check_batch(h_a, h_b, h_r, limbs, kAddMaxLimbs64, "host_add"));
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
     const size_t row = size_t(limbs) * 8;
-    return host_pipeline(ctx, h_a, h_b, h_r, h_carry, n, row, row,
+    return host_pipeline(ctx, HOST_ADD, h_a, h_b, h_r, h_carry, n, row, row,
                          [limbs, tb = add_bytes(ctx, limbs, 8)](void* da, void* db, void* dr, uint8_t* dc,
                                                                  uint32_t cnt, cudaStream_t st) {
                              return launch_add_u64(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
@@ -540,7 +599,7 @@ mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* 
     MI_TRY(check_batch(h_a, h_b, h_r, limbs, kMulMaxN32 / 2, "host_mul_full"));
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
     const size_t row = size_t(limbs) * 8;
-    return host_pipeline(ctx, h_a, h_b, h_r, nullptr, n, row, 2 * row,
+    return host_pipeline(ctx, HOST_MUL, h_a, h_b, h_r, nullptr, n, row, 2 * row,
                          [limbs](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                        static_cast<uint32_t*>(dr), cnt, 2 * limbs, true, st);

@@ -12,10 +12,17 @@ struct mi_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
     mi::NttTables ntt;  // resident twiddles of the three NTT primes
-    // host-pointer pipeline: two streams, each with its own device staging area
-    cudaStream_t pipe[2] = {nullptr, nullptr};
-    void* stage[2] = {nullptr, nullptr};
+    // host-pointer pipeline: a copy-in stream, a copy-out stream and two
+    // compute streams over a ring of staging slots, ordered by events
+    static constexpr int kSlots = 3;
+    cudaStream_t pipe[4] = {};  // 0 copy-in, 1 copy-out, 2 and 3 compute
+    cudaEvent_t ev_in[kSlots] = {}, ev_k[kSlots] = {}, ev_out[kSlots] = {};
+    void* stage[kSlots] = {};
     size_t stage_cap = 0;
+    // by operation class (0 additions, 1 multiplications): chunks of a large
+    // host-buffer batch, and whether kernels read mapped pinned buffers in place
+    uint32_t host_chunks[2] = {mi::tuned::kHostChunks[0], mi::tuned::kHostChunks[1]};
+    uint32_t host_zero_copy[2] = {mi::tuned::kHostZeroCopy[0], mi::tuned::kHostZeroCopy[1]};
     std::mutex mu;  // serialises host-pointer calls on one context
     // ragged batches: products whose shorter operand has at least this many
     // u64 limbs go through the NTT kernel (at most 129: classical groups hold

@@ -17,6 +17,11 @@ constexpr uint32_t kRaggedNttMin = 128;
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32, 32, 64, 64};
+// Host-buffer calls, by operation class {additions, multiplications}: chunks a
+// large batch is cut into for copy/compute overlap, and whether kernels read
+// mapped pinned host buffers in place (1) instead.
+constexpr uint32_t kHostChunks[2] = {4, 1};
+constexpr uint32_t kHostZeroCopy[2] = {0, 1};
 
 }  // namespace tuned
 }  // namespace mi

@@ -33,7 +33,7 @@ RAGGED_NOALLOC_MAX_OPS = 65536
 # Every symbol include/midint.h declares, with (restype, argtypes).
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
 _S = ctypes.c_int  # mi_status
-TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES = 0, 1, 2
+TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES, TUNE_HOST_CHUNKS, TUNE_HOST_ZERO_COPY = 0, 1, 2, 3, 4
 SIGNATURES = {
     "mi_version": (_I, []),
     "mi_status_string": (ctypes.c_char_p, [_I]),

@@ -1,0 +1,92 @@
+"""Host-buffer calls (mi_host_*): every chunking of the copy/compute pipeline
+and the zero-copy path on mapped pinned buffers give the oracle's results."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import midint
+import oracle as O
+from carry_data import carry_stress
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(x: np.ndarray) -> torch.Tensor:
+    t = torch.from_numpy(x.view(np.int64) if x.dtype == np.uint64 else x).pin_memory()
+    return t
+
+
+@pytest.fixture
+def hctx(lib):
+    c = midint.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 8, 64])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_mul_full_chunkings(hctx, chunks, pinned):
+    n, m = 1000, 64
+    a, b = carry_stress(n, m, seed=chunks)
+    hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 1, chunks)
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 0)
+    want = O.mul(a, b, m, True)
+    if pinned:
+        pa, pb = _pinned(a), _pinned(b)
+        pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+        hctx.host_mul_full(pa, pb, pr, n, m)
+        got = pr.numpy().view(np.uint64)
+    else:
+        got = np.zeros(2 * n * m, np.uint64)
+        hctx.host_mul_full(a, b, got, n, m)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("chunks", [1, 5, 16])
+def test_host_add_chunkings(hctx, chunks):
+    n, m = 3001, 33
+    a, b = carry_stress(n, m, seed=chunks + 100)
+    hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 0, chunks)
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 0)
+    r = np.zeros(n * m, np.uint64)
+    c = np.zeros(n, np.uint8)
+    hctx.host_add(a, b, r, c, n, m)
+    ra, ca = O.add(a, b, m)
+    assert np.array_equal(r, ra) and np.array_equal(c, ca)
+
+
+def test_zero_copy_on_pinned_buffers(hctx):
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 1)
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 1)
+    n, m = 777, 128
+    a, b = carry_stress(n, m, seed=9)
+    pa, pb = _pinned(a), _pinned(b)
+    pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+    hctx.host_mul_full(pa, pb, pr, n, m)
+    assert np.array_equal(pr.numpy().view(np.uint64), O.mul(a, b, m, True))
+    na, ma = 2049, 64
+    a, b = carry_stress(na, ma, seed=10)
+    pa, pb = _pinned(a), _pinned(b)
+    pr = torch.zeros(na * ma, dtype=torch.int64).pin_memory()
+    pc = torch.zeros(na, dtype=torch.uint8).pin_memory()
+    hctx.host_add(pa, pb, pr, pc, na, ma)
+    ra, ca = O.add(a, b, ma)
+    assert np.array_equal(pr.numpy().view(np.uint64), ra) and np.array_equal(pc.numpy(), ca)
+    # pageable buffers fall back to the copy pipeline
+    r = np.zeros(na * ma, np.uint64)
+    c = np.zeros(na, np.uint8)
+    hctx.host_add(a, b, r, c, na, ma)
+    assert np.array_equal(r, ra) and np.array_equal(c, ca)
+
+
+def test_host_tuning_knobs_are_checked(hctx):
+    with pytest.raises(midint.MidintError):
+        hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 0, 0)
+    with pytest.raises(midint.MidintError):
+        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 2)
+    with pytest.raises(midint.MidintError):
+        hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 2, 4)
+    hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 1, 5)
+    assert hctx.get_tuning(midint.TUNE_HOST_CHUNKS, 1) == 5
