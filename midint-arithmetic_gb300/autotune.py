@@ -155,7 +155,8 @@ def tune_host(ctx) -> tuple[list[int], list[int], dict]:
     """Host-buffer calls on pinned buffers, wall-clock per call, for every chunk
     count and with zero-copy: class 0 on the addition batch (65536 x 64 u64
     limbs, with carries), class 1 on the classical multiplication batch (16384
-    x 128 u64 limbs, full products).  Each class takes its fastest choice."""
+    x 128 u64 limbs, full products).  Each class takes its fastest chunk count
+    and zero-copy where it beats that."""
     import time
 
     import torch
@@ -186,12 +187,15 @@ def tune_host(ctx) -> tuple[list[int], list[int], dict]:
             ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
             ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
             cands[f"zero_copy={zc},chunks={ch}"] = {"zero_copy": zc, "chunks": ch, "ms": wall(calls[cls])}
-        best = min(cands.values(), key=lambda v: v["ms"])
-        ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, best["zero_copy"])
-        ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, best["chunks"])
-        chunks.append(best["chunks"])
-        zero_copy.append(best["zero_copy"])
-        record[name] = {"candidates": cands, "pick": best}
+        # the chunk count serves callers whose buffers are not pinned even
+        # when zero-copy wins for pinned ones
+        best_copy = min((v for v in cands.values() if not v["zero_copy"]), key=lambda v: v["ms"])
+        zc = int(cands["zero_copy=1,chunks=1"]["ms"] < best_copy["ms"])
+        ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
+        ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, best_copy["chunks"])
+        chunks.append(best_copy["chunks"])
+        zero_copy.append(zc)
+        record[name] = {"candidates": cands, "pick": {"chunks": best_copy["chunks"], "zero_copy": zc}}
     return chunks, zero_copy, record
 
 

@@ -20,7 +20,7 @@ constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32,
 // Host-buffer calls, by operation class {additions, multiplications}: chunks a
 // large batch is cut into for copy/compute overlap, and whether kernels read
 // mapped pinned host buffers in place (1) instead.
-constexpr uint32_t kHostChunks[2] = {4, 1};
+constexpr uint32_t kHostChunks[2] = {4, 3};
 constexpr uint32_t kHostZeroCopy[2] = {0, 1};
 
 }  // namespace tuned
