@@ -250,6 +250,21 @@ __global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
 
 // --- classical family ----------------------------------------------------------
 
+// Thread t's two 16-byte slots (t and t+NT) of the W = NT*T limbs of x
+// starting at limb `start`, zero beyond nx (x rows are 8-byte aligned).
+template <int NT>
+__device__ __forceinline__ void load_chunk_regs(uint4 (&q)[classic::T / 4], const uint32_t* __restrict__ x,
+                                                uint32_t nx, uint32_t start, uint32_t t) {
+#pragma unroll
+    for (int it = 0; it < classic::T / 4; ++it) {
+        const uint32_t w = start + 4 * (t + uint32_t(it) * NT);
+        uint2 lo = make_uint2(0, 0), hi = make_uint2(0, 0);
+        if (w + 2 <= nx) lo = __ldcs(reinterpret_cast<const uint2*>(x + w));
+        if (w + 4 <= nx) hi = __ldcs(reinterpret_cast<const uint2*>(x + w + 2));
+        q[it] = make_uint4(lo.x, lo.y, hi.x, hi.y);
+    }
+}
+
 template <int NT>
 __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* wsm) {
     using classic::T;
@@ -274,9 +289,13 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     uint32_t pend[T];
 #pragma unroll
     for (int w = 0; w < T; ++w) pend[w] = 0;
+    // chunk c+1 of x is loaded into registers while chunk c is multiplied
+    uint4 nxt[T / 4];
+    load_chunk_regs<NT>(nxt, x, nx, 0, t);
     for (uint32_t c = 0; c < chunks; ++c) {
-        const uint32_t left = nx - c * W;
-        classic::stage_a<NT, false>(gA, x + c * W, left < W ? left : W, true, t);
+#pragma unroll
+        for (int it = 0; it < T / 4; ++it) reinterpret_cast<uint4*>(gA)[t + it * NT] = nxt[it];
+        if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
         classic::square_product<NT>(gA, gB4, slots, nullptr, t, ulo, uhi);
@@ -411,7 +430,10 @@ mi_status init_device() {
     for (int k = 0; k < K_NTT; ++k) order[KEY_NTT + k] = uint16_t(KEY_NTT + (K_NTT - 1 - k));
     std::vector<int> cls(K_CLS);
     for (int k = 0; k < K_CLS; ++k) cls[k] = k;
-    auto cost = [](int k) { return (1 << (k / 256)) * (k % 256 + 1); };  // NT x chunks
+    // a chunk costs its NT tile steps plus a fixed overhead (operand load,
+    // carry passes, store) worth about kChunkOverhead steps
+    constexpr int kChunkOverhead = 8;
+    auto cost = [](int k) { return ((1 << (k / 256)) + kChunkOverhead) * (k % 256 + 1); };
     std::stable_sort(cls.begin(), cls.end(), [&](int x, int y) { return cost(x) > cost(y); });
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));

@@ -1,0 +1,96 @@
+"""One launch of each kernel family on the benchmark's shapes, for profilers.
+
+Runs, on cuda:0, each selected operation once (after one untimed warm-up call
+when --warmup 1) with seeded inputs already resident on the device:
+
+  add     65536 x 64 u64 limbs, carries        (k_add)
+  add6    6a + 10b on the same batch            (k_add, 6a+10b variant)
+  mul     16384 x 128 u64 limbs, full products  (k_mul)
+  mul_lo  the same batch, low halves            (k_mul_lo)
+  poly    the same batch                        (k_poly)
+  ntt     1024 x 1024 u64 limbs                 (k_ntt_mul)
+  ragged  a mixed ragged list (--ragged-ops)    (k_classify, k_scan, k_scatter, k_rg_*)
+
+Usage: python midint-arithmetic_gb300/profcase.py [--ops add,mul,...] [--warmup 0|1]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ops", default="add,add6,mul,mul_lo,poly,ntt,ragged")
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--ragged-ops", type=int, default=20000)
+    args = ap.parse_args()
+
+    import torch
+
+    import midint
+    import workloads
+
+    dev = torch.device("cuda:0")
+    ctx = midint.Context(0)
+    sp = torch.cuda.current_stream().cuda_stream
+
+    def dput(x):
+        return torch.from_numpy(x.view(np.int64)).to(dev)
+
+    calls = []
+    ops = args.ops.split(",")
+    if "add" in ops or "add6" in ops:
+        a, b = workloads.add_pairs(n=65536, m=64)
+        da, db = dput(a), dput(b)
+        dr = torch.empty_like(da)
+        dc = torch.empty(65536, dtype=torch.uint8, device=dev)
+        if "add" in ops:
+            calls.append(lambda: ctx.add(da, db, dr, 65536, 64, carry=dc, stream=sp))
+        if "add6" in ops:
+            calls.append(lambda: ctx.add6(da, db, dr, 65536, 64, stream=sp))
+    if any(o in ops for o in ("mul", "mul_lo", "poly")):
+        a, b = workloads.mul_pairs(n=16384, m=128)
+        ma, mb = dput(a), dput(b)
+        mr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        if "mul" in ops:
+            calls.append(lambda: ctx.mul_full(ma, mb, mr, 16384, 128, stream=sp))
+        if "mul_lo" in ops:
+            calls.append(lambda: ctx.mul_lo(ma, mb, mr, 16384, 128, stream=sp))
+        if "poly" in ops:
+            calls.append(lambda: ctx.poly(ma, mb, mr, 16384, 128, stream=sp))
+    if "ntt" in ops:
+        a, b = workloads.ntt_pairs(n=1024, m=1024)
+        na, nb = dput(a), dput(b)
+        nr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        calls.append(lambda: ctx.mul_ntt(na, nb, nr, 1024, 1024, stream=sp))
+    if "ragged" in ops:
+        rops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops)
+        d_ops = torch.from_numpy(rops.view(np.uint8).copy()).to(dev)
+        d_in = dput(pool)
+        d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+        d_c = torch.empty(rops.size, dtype=torch.uint8, device=dev)
+        sb = midint.ragged_scratch_bytes(rops.size)
+        scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+        calls.append(lambda: ctx.ragged_run(d_ops, rops.size, d_in, d_out, scr, sb, carry=d_c, stream=sp))
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        for c in calls:
+            c()
+    torch.cuda.synchronize()
+    for c in calls:
+        c()
+    torch.cuda.synchronize()
+    ctx.close()
+    print("profcase: ran", ",".join(ops))
+
+
+if __name__ == "__main__":
+    main()
