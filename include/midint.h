@@ -48,9 +48,11 @@ typedef struct mi_ctx_s* mi_ctx;
 /* A cudaStream_t passed as a plain pointer (NULL = CUDA's default stream). */
 typedef void* mi_stream;
 
-/* Largest operand length, in u64 limbs, that any single-instance kernel takes
- * (65536 bits).  u32 entry points accept twice as many limbs. */
-#define MI_MAX_LIMBS_U64 1024u
+/* Largest operand length, in u64 limbs, of the plain multiplication kernels
+ * (classical, NTT, poly): 131072 bits, the largest size the reference's
+ * drivers run (cuda/main.cu:693-703).  u32 entry points accept twice as many
+ * limbs; additions take up to 4096 u64 limbs; ragged ops up to 1024. */
+#define MI_MAX_LIMBS_U64 2048u
 
 /* ---------------------------------------------------------------------------
  * Library / context
@@ -121,9 +123,10 @@ mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t*
 mi_status mi_add_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r,
                      uint8_t* carry_out, uint32_t n, uint32_t limbs, mi_stream stream);
 
-/* Fused six-addition composite r = 6a + 10b (mod 2^(bits*limbs)) with the
- * reference's chain t1=a+b, t2=2t1, t3=t2+b, t4=2t3, t5=t4+t3, r=t5+b held in
- * registers.  Replaces a6pb10Ker (cuda/ker-addition.cu.h:266-328). */
+/* Fused six-addition composite r = 6a + 10b (mod 2^(bits*limbs)), the value of
+ * the reference's chain t1=a+b, t2=2t1, t3=t2+b, t4=2t3, t5=t4+t3, r=t5+b,
+ * formed per limb as 6a_i + 10b_i with one carry pass.  Replaces a6pb10Ker
+ * (cuda/ker-addition.cu.h:266-328). */
 mi_status mi_add6_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
                       uint32_t n, uint32_t limbs, mi_stream stream);
 
@@ -145,13 +148,13 @@ mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint
                           uint32_t n, uint32_t limbs, mi_stream stream);
 
 /* Fused polynomial composite r = ((a^2 + b)(b^2 + b) + ab) mod 2^(64*limbs),
- * every intermediate mod 2^(64*limbs) and held on chip, limbs <= 1024.
+ * every intermediate mod 2^(64*limbs) and held on chip, limbs <= 2048.
  * Replaces polyKerQ (cuda/ker-classic-mul.cu.h:500-575). */
 mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
                       uint32_t n, uint32_t limbs, mi_stream stream);
 
 /* ---------------------------------------------------------------------------
- * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 1024: every u64
+ * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 2048: every u64
  * limb is one digit, three 62-bit primes (the first is the reference's
  * FftPrime64, 29*2^57+1) carry the convolution, Garner's CRT and the final
  * carry run in the same kernel.  Replaces bmulFFT<P,M,Q>
@@ -187,7 +190,8 @@ mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_
  * u32 words per instance), exactly where the reference's kernel writes them
  * (cuda/ker-fft-mul.cu.h:451-452).  This is the exact result the reference's
  * disabled validation expects (cuda/main.cu:598-608).  M must be a multiple
- * of 4 and at most 4096. */
+ * of 4 and at most 8192 (the largest M the reference's kernel can launch:
+ * M/8 threads per block at its Q = 4). */
 mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t* h_as,
                                   const uint16_t* h_bs, uint32_t* h_rs);
 
@@ -321,7 +325,7 @@ mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s, double* se
  * natural order (the reference's fft, cuda/ker-fft-mul.cu.h:304-348), conv = 1
  * the cyclic convolution of a and b mod p (bmulFFTvalid,
  * cuda/ker-fft-mul.cu.h:512-554).  p odd < 2^62, g of order 2^two_adicity
- * (two_adicity >= 11), len a power of two in [8, 2048]; host buffers of len
+ * (two_adicity >= 12), len a power of two in [8, 2048]; host buffers of len
  * words; synchronous.  Used to check the transform against the reference's
  * known answers.
  * ------------------------------------------------------------------------- */

@@ -42,7 +42,7 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
                         uint8_t* carry, void* scratch, size_t scratch_bytes, uint32_t ntt_min, cudaStream_t st);
 
 // Largest u32 limb count the classical kernel takes per instance.
-constexpr uint32_t kMulMaxN32 = 2048;
+constexpr uint32_t kMulMaxN32 = 4096;
 // Largest u64 limb count the addition kernels take per instance (one group of
 // at most 1024 threads, 4 limbs each).
 constexpr uint32_t kAddMaxLimbs64 = 4096;

@@ -29,7 +29,7 @@ struct MulShape {
 };
 
 template <int NT, bool VEC>
-__global__ void __launch_bounds__(NT > 256 ? NT : 256, NT == 2 ? 2 : 3)
+__global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 ? 2 : 3))
     k_mul(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ r, uint32_t n,
           uint32_t n32, bool full) {
     using S = MulShape<NT>;
@@ -105,6 +105,7 @@ mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n
         case 64: return launch_nt<64, VEC>(a, b, r, n, n32, full, st);
         case 128: return launch_nt<128, VEC>(a, b, r, n, n32, full, st);
         case 256: return launch_nt<256, VEC>(a, b, r, n, n32, full, st);
+        case 512: return launch_nt<512, VEC>(a, b, r, n, n32, full, st);
         default: return set_error(MI_EINVAL, "mul: %u u32 limbs exceeds the classical maximum", n32);
     }
 }

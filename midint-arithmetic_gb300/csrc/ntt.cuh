@@ -25,10 +25,10 @@
 // bit-reversal permutation with a barrier per element, and reads each twiddle
 // from global memory (fft/ifft, cuda/ker-fft-mul.cu.h:304-368).
 //
-// Twiddles: tw[e] = w^e * R mod p and itw[e] = w^-e * R mod p for e < 1024,
-// w a primitive 2048th root of unity (the reference's getOmega convention,
-// w = g^(2^(s - 11)), cuda/ker-fft-mul.cu.h:191-199); a length-L transform
-// reads every (2048/L)-th entry.
+// Twiddles: tw[e] = w^e * R mod p and itw[e] = w^-e * R mod p for e < 2048,
+// w a primitive 4096th root of unity (the reference's getOmega convention,
+// w = g^(2^(s - lg)), cuda/ker-fft-mul.cu.h:191-199, at lg = 12); a length-L
+// transform reads every (4096/L)-th entry.
 #pragma once
 
 #include <cstdint>
@@ -36,7 +36,7 @@
 namespace mi {
 namespace ntt {
 
-constexpr int kLgMax = 11;                 // 2048-point transforms at most
+constexpr int kLgMax = 12;                 // 4096-point transforms at most
 constexpr int kTwiddles = (1 << kLgMax) / 2;
 
 struct FieldC32 {

@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "ntt.cuh"
 #include "ntt_host.h"
 
 namespace mi {
@@ -34,11 +35,11 @@ uint64_t host_invmod(uint64_t a, uint64_t p) { return host_powmod(a, p - 2, p); 
 static uint64_t r_mod(uint64_t p) { return uint64_t(((u128)1 << 64) % p); }
 
 void host_twiddles(uint64_t p, uint64_t g, uint32_t s, uint64_t* tw, uint64_t* itw) {
-    const uint64_t w = host_powmod(g, uint64_t(1) << (s - 11), p);  // order 2048
+    const uint64_t w = host_powmod(g, uint64_t(1) << (s - ntt::kLgMax), p);  // order 2^kLgMax
     const uint64_t wi = host_invmod(w, p);
     const uint64_t R = r_mod(p);
     uint64_t acc = R, acci = R;  // w^0 * R
-    for (int e = 0; e < (1 << 11) / 2; ++e) {
+    for (int e = 0; e < ntt::kTwiddles; ++e) {
         tw[e] = acc;
         itw[e] = acci;
         acc = host_mulmod(acc, w, p);
@@ -47,7 +48,7 @@ void host_twiddles(uint64_t p, uint64_t g, uint32_t s, uint64_t* tw, uint64_t* i
 }
 
 mi_status ntt_tables_create(NttTables* T) {
-    constexpr int E = (1 << 11) / 2;
+    constexpr int E = ntt::kTwiddles;
     std::vector<uint64_t> h(size_t(6) * E);
     NttMulParams& P = T->params;
     std::memset(&P, 0, sizeof(P));
@@ -58,7 +59,7 @@ mi_status ntt_tables_create(NttTables* T) {
         P.c[q] = uint32_t(p >> 32);
         const uint64_t R = r_mod(p);
         P.kb[q] = host_mulmod(R, R, p);
-        for (int lg = 0; lg < 12; ++lg) P.ka_by_lg[q][lg] = host_mulmod(R, host_invmod(uint64_t(1) << lg, p), p);
+        for (int lg = 0; lg <= ntt::kLgMax; ++lg) P.ka_by_lg[q][lg] = host_mulmod(R, host_invmod(uint64_t(1) << lg, p), p);
     }
     const uint64_t q0 = kNttPrimes[0].p, q1 = kNttPrimes[1].p, q2 = kNttPrimes[2].p;
     P.g01 = host_mulmod(host_invmod(q0 % q1, q1), r_mod(q1), q1);
@@ -89,9 +90,9 @@ extern "C" mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, ui
                                 const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_out) {
     if (h_a == nullptr || h_out == nullptr || (conv && h_b == nullptr)) return set_error(MI_EINVAL, "ntt_raw: null");
     if (len < 8 || len > 2048 || (len & (len - 1))) return set_error(MI_EINVAL, "ntt_raw: bad length %u", len);
-    if ((p & 1) == 0 || p >= (uint64_t(1) << 62) || two_adicity < 11 || two_adicity > 63)
-        return set_error(MI_EINVAL, "ntt_raw: prime must be odd, < 2^62, with 2-adicity >= 11");
-    constexpr int E = (1 << 11) / 2;
+    if ((p & 1) == 0 || p >= (uint64_t(1) << 62) || two_adicity < uint32_t(ntt::kLgMax) || two_adicity > 63)
+        return set_error(MI_EINVAL, "ntt_raw: prime must be odd, < 2^62, with 2-adicity >= %d", ntt::kLgMax);
+    constexpr int E = ntt::kTwiddles;
     std::vector<uint64_t> tw(2 * E);
     host_twiddles(p, g, two_adicity, tw.data(), tw.data() + E);
     NttRawArgs A{};

@@ -8,7 +8,7 @@
 
 namespace mi {
 
-constexpr uint32_t kNttMaxLimbs = 1024;  // u64 limbs per operand (2048-point transforms)
+constexpr uint32_t kNttMaxLimbs = 2048;  // u64 limbs per operand (4096-point transforms)
 
 // One NTT prime: p = c*2^32 + 1 < 2^62, g of multiplicative order exactly 2^s
 // (the reference's FftPrime convention, cuda/ker-fft-mul.cu.h:44-72).
@@ -31,14 +31,14 @@ struct NttMulParams {
     uint32_t c[3];
     uint64_t ka[3];            // R/L mod p for the launch's transform length
     uint64_t kb[3];            // R^2 mod p
-    uint64_t ka_by_lg[3][12];  // R/2^lg mod p
-    const uint64_t* tw[3];     // w^e R mod p, e < 1024
+    uint64_t ka_by_lg[3][13];  // R/2^lg mod p, lg <= 12
+    const uint64_t* tw[3];     // w^e R mod p, e < 2048
     const uint64_t* itw[3];    // w^-e R mod p
     uint64_t g01, g02, g12;    // Garner constants q0^-1 mod q1, q0^-1 mod q2, q1^-1 mod q2 (times R)
     uint64_t q01_lo, q01_hi;   // q0*q1
 };
 
-// Device-resident tables of one context (48 KiB) and the parameter block.
+// Device-resident tables of one context (96 KiB) and the parameter block.
 struct NttTables {
     uint64_t* d_tw = nullptr;
     NttMulParams params{};
@@ -72,8 +72,8 @@ mi_status launch_ntt_raw(const NttRawArgs& A, cudaStream_t st);
 uint64_t host_mulmod(uint64_t a, uint64_t b, uint64_t p);
 uint64_t host_powmod(uint64_t a, uint64_t e, uint64_t p);
 uint64_t host_invmod(uint64_t a, uint64_t p);  // p prime
-// Fills tw/itw (1024 entries each, Montgomery form) for a prime with a
-// generator of order 2^s, s >= 11.
+// Fills tw/itw (2048 entries each, Montgomery form) for a prime with a
+// generator of order 2^s, s >= 12.
 void host_twiddles(uint64_t p, uint64_t g, uint32_t s, uint64_t* tw, uint64_t* itw);
 
 }  // namespace mi

@@ -6,7 +6,7 @@
 // prime from 16 digits on, and cuda/main.cu:729-739 disables validation).
 //
 // Here every u64 limb is one digit; the product of two m-limb integers has
-// coefficients below m * 2^128 <= 2^138 (m <= 1024), so three primes
+// coefficients below m * 2^128 <= 2^139 (m <= 2048), so three primes
 // q0 < q1 < q2 < 2^62 (product 2^186) recover every coefficient exactly by
 // CRT.  One CTA of L/8 threads owns one instance (L = pow2ceil(2m) >= 256):
 // for each prime it converts a and b into the field (a scaled by 1/L, so the
@@ -39,7 +39,8 @@ struct NttShape {
     static constexpr size_t SMEM = ntt::MulSmem<LG>::WORDS64 * 8 + size_t(NT / 32 + 1) * 4;
 };
 
-// 768 threads per SM: three 256-thread CTAs for 2048-point transforms
+// 768 threads per SM: three 256-thread CTAs for 2048-point transforms (one
+// 512-thread CTA for 4096-point ones)
 template <int LG>
 __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     k_ntt_mul(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ r, uint32_t n,
@@ -121,6 +122,7 @@ mi_status launch_mul_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
         case 512: return launch_lg<9>(a, b, r, n, m, rlen, P, st);
         case 1024: return launch_lg<10>(a, b, r, n, m, rlen, P, st);
         case 2048: return launch_lg<11>(a, b, r, n, m, rlen, P, st);
+        case 4096: return launch_lg<12>(a, b, r, n, m, rlen, P, st);
         default: return set_error(MI_EINVAL, "ntt: %u limbs exceeds the maximum %u", m, kNttMaxLimbs);
     }
 }

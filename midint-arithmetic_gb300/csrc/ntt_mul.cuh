@@ -2,7 +2,7 @@
 // (shared by the batched kernel in ntt_mul.cu and the ragged kernels).
 //
 // Every u64 limb is one digit; the product of an la-limb and an lb-limb
-// integer has coefficients below min(la, lb) * 2^128 <= 2^138 (limbs <= 1024),
+// integer has coefficients below min(la, lb) * 2^128 <= 2^139 (limbs <= 2048),
 // so three primes q0 < q1 < q2 < 2^62 (product 2^186) recover every coefficient
 // exactly by CRT.  For each prime the group converts a and b into the field
 // (a scaled by 1/L, so the inverse transform needs no scaling pass), runs two

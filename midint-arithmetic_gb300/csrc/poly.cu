@@ -149,7 +149,7 @@ mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n
         return launch_lo<NH>(k_poly<NH, VEC>, attr_done, a, b, r, n, n32, st);           \
     }
         MI_LO_CASE(1) MI_LO_CASE(2) MI_LO_CASE(4) MI_LO_CASE(8) MI_LO_CASE(16) MI_LO_CASE(32) MI_LO_CASE(64)
-        MI_LO_CASE(128)
+        MI_LO_CASE(128) MI_LO_CASE(256)
 #undef MI_LO_CASE
         default: return set_error(MI_EINVAL, "poly: %u u32 limbs exceeds the classical maximum", n32);
     }

@@ -27,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmidint_gb300.so")
 
 MI_OK, MI_EINVAL, MI_ENOMEM, MI_ECUDA, MI_ETIMEOUT, MI_ENODEV, MI_ENOTSUP = range(7)
-MAX_LIMBS_U64 = 1024
+MAX_LIMBS_U64 = 2048
 RAGGED_NOALLOC_MAX_OPS = 65536
 
 # Every symbol include/midint.h declares, with (restype, argtypes).
@@ -208,7 +208,7 @@ class Context:
         check(load().mi_poly_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
 
     def mul_ntt(self, a, b, r, n: int, limbs: int, stream=None) -> None:
-        """Exact full product by NTT (u64 limbs, limbs <= 1024)."""
+        """Exact full product by NTT (u64 limbs, limbs <= 2048)."""
         check(load().mi_mul_ntt_u64(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
 
     def mul(self, a, b, r, n: int, limbs: int, stream=None) -> None:

@@ -31,7 +31,8 @@ def gpu_mul(ctx, devmem, a, b, m, full=True, limb_bits=64, offset=0):
     return devmem.get(br, out_words, offset, a.dtype)
 
 
-U64_SIZES = [1, 2, 3, 4, 5, 8, 15, 16, 17, 31, 32, 33, 64, 100, 128, 129, 200, 256, 500, 512, 1000, 1024]
+U64_SIZES = [1, 2, 3, 4, 5, 8, 15, 16, 17, 31, 32, 33, 64, 100, 128, 129, 200, 256, 500, 512, 1000, 1024, 1025,
+             1500, 2047, 2048]
 
 
 @pytest.mark.parametrize("m", U64_SIZES)
@@ -42,7 +43,7 @@ def test_mul_u64_matches_oracle(ctx, devmem, m, full):
     assert np.array_equal(gpu_mul(ctx, devmem, a, b, m, full), O.mul(a, b, m, full))
 
 
-@pytest.mark.parametrize("m", [1, 3, 7, 9, 15, 255, 257, 511, 2047])
+@pytest.mark.parametrize("m", [1, 3, 7, 9, 15, 255, 257, 511, 2047, 4095])
 @pytest.mark.parametrize("full", [True, False])
 def test_mul_u32_odd_sizes(ctx, devmem, m, full):
     n = 11
@@ -58,7 +59,7 @@ def test_mul_unaligned(ctx, devmem, m):
         assert np.array_equal(got.view(np.uint64), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [16, 32, 64, 128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("m", [16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
 def test_mul_matches_reference_fixtures(ctx, devmem, m):
     g = golden("ref_sweep.npz")
     assert np.array_equal(gpu_mul(ctx, devmem, g["a"], g["b"], m, full=False, limb_bits=32), g[f"mul_{m}"])
@@ -73,7 +74,7 @@ def test_mul_matches_reference_fixtures(ctx, devmem, m):
 
 
 def test_mul_all_ones_full(ctx, devmem):
-    for m in (1, 64, 128, 1024):
+    for m in (1, 64, 128, 1024, 2048):
         a = np.full(3 * m, 0xFFFFFFFFFFFFFFFF, np.uint64)
         assert np.array_equal(gpu_mul(ctx, devmem, a, a, m, True), O.mul(a, a, m, True))
 
@@ -91,7 +92,7 @@ def test_mul_config_shape(ctx, devmem):
 
 def test_compat_gpuMultiply(lib):
     g = golden("ref_sweep.npz")
-    for m in (16, 256, 2048):
+    for m in (16, 256, 2048, 4096):
         r = np.zeros_like(g["a"])
         midint.gpuMultiply(midint.U32bits, m, g["a"].size // m, g["a"], g["b"], r)
         assert np.array_equal(r, g[f"mul_{m}"])

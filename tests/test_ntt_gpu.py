@@ -64,7 +64,8 @@ def gpu_mul_ntt(ctx, devmem, a, b, m, via="ntt"):
     return devmem.get(br, 4 * a.size)
 
 
-NTT_SIZES = [1, 2, 3, 63, 64, 65, 100, 127, 128, 129, 255, 256, 257, 500, 511, 512, 513, 1000, 1023, 1024]
+NTT_SIZES = [1, 2, 3, 63, 64, 65, 100, 127, 128, 129, 255, 256, 257, 500, 511, 512, 513, 1000, 1023, 1024, 1025,
+             1500, 2047, 2048]
 
 
 @pytest.mark.parametrize("m", NTT_SIZES)
@@ -74,7 +75,7 @@ def test_mul_ntt_matches_oracle(ctx, devmem, m):
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [64, 256, 1024])
+@pytest.mark.parametrize("m", [64, 256, 1024, 2048])
 def test_mul_ntt_maximal_coefficients(ctx, devmem, m):
     # all-ones operands give the largest convolution coefficients (~m * 2^128)
     a = np.full(3 * m, 0xFFFFFFFFFFFFFFFF, np.uint64)
@@ -83,7 +84,7 @@ def test_mul_ntt_maximal_coefficients(ctx, devmem, m):
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [1, 100, 255, 256, 700, 1024])
+@pytest.mark.parametrize("m", [1, 100, 255, 256, 700, 1024, 2048])
 def test_mul_dispatch_matches_oracle(ctx, devmem, m):
     a, b = carry_stress(5, m, seed=m + 3)
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m, via="dispatch"), O.mul(a, b, m, True))
@@ -110,7 +111,7 @@ def test_mul_ntt_matches_classical_on_reference_fixtures(ctx, devmem):
 
 def test_compat_gpuMulFFT(lib):
     g = golden("ref_sweep.npz")
-    for m32 in (64, 256, 2048):
+    for m32 in (64, 256, 2048, 4096):
         M = 2 * m32                                # u16 digits
         a16 = g["a"].view(np.uint16)
         b16 = g["b"].view(np.uint16)

@@ -29,7 +29,7 @@ def gpu_poly(ctx, devmem, a, b, m, offset=0):
     return devmem.get(br, words, offset)
 
 
-@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 8, 16, 17, 32, 33, 64, 100, 128, 256, 257, 512, 1024])
+@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 8, 16, 17, 32, 33, 64, 100, 128, 256, 257, 512, 1024, 1500, 2048])
 def test_poly_matches_oracle(ctx, devmem, m):
     n = 41 if m <= 128 else 6
     a, b = carry_stress(n, m, seed=7 * m + 3)
@@ -58,5 +58,5 @@ def test_poly_rejects_bad_arguments(ctx):
     with pytest.raises(midint.MidintError):
         ctx.poly(0, 16, 32, 1, 4)
     with pytest.raises(midint.MidintError):
-        ctx.poly(16, 16, 16 + 8, 1, 1025)
+        ctx.poly(16, 16, 16 + 8, 1, 2049)
     ctx.poly(16, 16, 4096, 0, 4)  # empty batch: nothing launched
