@@ -106,9 +106,24 @@ enum {
     MI_TUNE_RAGGED_NTT_MIN = 1,
     MI_TUNE_ADD_THREAD_BYTES = 2,
     MI_TUNE_HOST_CHUNKS = 3,
-    MI_TUNE_HOST_ZERO_COPY = 4
+    MI_TUNE_HOST_ZERO_COPY = 4,
+    MI_TUNE_WIDE_SPIN_LIMIT = 5, /* cls ignored; polls of an unpublished
+                                  * predecessor before a multi-block addition
+                                  * gives up (default 2^20, about 70 ms) */
+    MI_TUNE_WIDE_WITHHOLD = 6,   /* cls ignored; 0 or 1.  Failure injection for
+                                  * tests: the first tile of every instance
+                                  * never publishes its carry, so the waits of
+                                  * its successors run out (bounded) */
+    MI_TUNE_WIDE_ROUND_TILES = 7 /* cls ignored; 1..65536: tiles (2048 u64 limbs
+                                  * each) per multi-block launch; an instance
+                                  * may not need more (default 65536) */
 };
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
+
+/* Waits for all work on the context's device, then reports (and clears) the
+ * context's device-side error state: MI_ETIMEOUT when a bounded wait of a
+ * multi-block addition gave up since the last report, else MI_OK. */
+mi_status mi_ctx_device_status(mi_ctx ctx);
 mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value);
 
 /* ---------------------------------------------------------------------------
@@ -117,6 +132,11 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
  * by gpuAdd (cuda/main.cu:39-119).  The reference discards the carry-out;
  * carry_out may be NULL to do the same.  a, b, r: n*limbs limbs each.
  * r may alias a or b exactly (in-place), but must not partially overlap.
+ * limbs <= 2^26 u64 limbs (2^27 u32): instances wider than 4096 u64 limbs run
+ * a multi-block kernel whose tiles chain their carries by decoupled
+ * look-back with bounded waits; such calls on one context must not overlap on
+ * the device, and a wait that gave up is reported by mi_ctx_device_status
+ * (and by the host-buffer calls) as MI_ETIMEOUT.
  * ------------------------------------------------------------------------- */
 mi_status mi_add_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
                      uint8_t* carry_out, uint32_t n, uint32_t limbs, mi_stream stream);

@@ -200,6 +200,148 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
     }
 }
 
+// --- instances wider than one block: decoupled look-back -------------------
+//
+// A tile is one 256-thread block over 64 bytes of each operand per thread
+// (2048 u64 limbs).  Tiles take their index from an atomic counter in launch
+// order, so every tile a tile waits for has already started and will finish
+// (no dependence on the scheduler).  Each tile adds its limbs with carry-in 0,
+// publishes its status word -- inclusive (its true carry-out) when it does not
+// propagate a carry or is the first tile of its instance, otherwise an
+// aggregate that says "passes the carry-in through" -- then thread 0 walks back
+// over aggregates to the nearest inclusive status, bounded by spin_limit polls
+// of an unpublished word (then the error word is set and the tile carries on
+// with carry-in 0, so the kernel always completes), publishes its own
+// inclusive status, and the block redoes the carry pass with that carry-in.
+// Status word: bits 0-1 state (1 aggregate, 2 inclusive), bit 2 carry value.
+
+constexpr uint32_t ST_AGG = 1u, ST_INC = 2u;
+
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <typename L, bool VEC, int OP>
+__global__ void __launch_bounds__(256)
+    k_add_wide(const L* __restrict__ a, const L* __restrict__ b, L* __restrict__ r, uint8_t* __restrict__ carry,
+               uint32_t m, uint32_t tiles_per, uint32_t n_tiles, uint32_t* status, uint32_t spin_limit,
+               uint32_t withhold) {
+    constexpr int Q = 64 / int(sizeof(L));
+    constexpr uint32_t W = 256u * Q;  // limbs per tile
+    __shared__ uint32_t scratch[8];
+    __shared__ uint64_t shift[8];
+    __shared__ uint32_t s_tile, s_cin;
+    uint32_t* counter = status + kWideTiles;
+    uint32_t* err = status + kWideTiles + 1;
+    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= n_tiles) return;  // (the grid has exactly n_tiles blocks)
+    const uint32_t inst = tile / tiles_per, j = tile % tiles_per;
+    const uint32_t t = threadIdx.x;
+    const uint64_t off = uint64_t(inst) * m;
+    const uint32_t start = j * W + t * Q;
+    L x[Q], y[Q], s[Q];
+    load_chunk<L, Q, VEC>(a + off, start, m, true, x);
+    load_chunk<L, Q, VEC>(b + off, start, m, true, y);
+    if constexpr (OP == ADD_SIX) {
+        // 6a + 10b as lo + (hi shifted up one limb), as in k_add; thread 0
+        // recomputes the high word of the limb before its tile
+        static_assert(sizeof(L) == 8, "6a + 10b is defined on u64 limbs");
+        L hi[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const L pa = x[q] * 6u, pb = y[q] * 10u;
+            const L lo = pa + pb;
+            hi[q] = __umul64hi(x[q], 6u) + __umul64hi(y[q], 10u) + L(lo < pa);
+            x[q] = lo;
+        }
+        uint64_t prev = group_shift_up<256>(hi[Q - 1], t, shift);
+        if (t == 0 && j > 0) {
+            const L xp = a[off + j * W - 1], yp = b[off + j * W - 1];
+            const L pa = xp * 6u, pb = yp * 10u;
+            prev = __umul64hi(xp, 6u) + __umul64hi(yp, 10u) + L(pa + pb < pa);
+        }
+        y[0] = prev;
+#pragma unroll
+        for (int q = 1; q < Q; ++q) y[q] = hi[q - 1];
+    }
+    bool g, p;
+    chunk_add<L, Q>(x, y, s, g, p);
+    uint32_t gc0;
+    (void)group_carry<256>(g, p, 0u, &gc0, scratch);
+    const bool P = __syncthreads_and(p) != 0;  // the tile passes a carry-in through
+    if (t == 0) {
+        uint32_t cin = 0;
+        if (j > 0) {
+            st_release(status + tile, P ? ST_AGG : (ST_INC | (gc0 << 2)));
+            uint32_t k = tile - 1, spins = 0;
+            for (;;) {
+                const uint32_t sv = ld_acquire(status + k);
+                if ((sv & 3u) == ST_INC) {
+                    cin = (sv >> 2) & 1u;
+                    break;
+                }
+                if ((sv & 3u) == ST_AGG) {  // a propagating tile that is not its instance's first
+                    --k;
+                    continue;
+                }
+                if (++spins > spin_limit) {
+                    atomicOr(err, 1u);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (!(withhold && j == 0)) st_release(status + tile, ST_INC | ((gc0 | (P ? cin : 0u)) << 2));
+        s_cin = cin;
+    }
+    __syncthreads();
+    uint32_t gc;
+    const uint32_t c = group_carry<256>(g, p, s_cin, &gc, scratch);
+    chunk_inc<L, Q>(s, c);
+    store_chunk<L, Q, VEC>(r + off, start, m, true, s);
+    if (OP == ADD_PLAIN && carry != nullptr && j == tiles_per - 1) {
+        // carry-out: the value at limb m (zero padding plus the carry), or
+        // the tile's carry-out when the instance ends with the tile
+        if (m % W != 0) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (start + q == m) carry[inst] = uint8_t(s[q]);
+        } else if (t == 255) {
+            carry[inst] = uint8_t(gc);
+        }
+    }
+}
+
+// Rounds of whole instances, at most kWideTiles tiles each; every round
+// clears its tile words and the counter first.
+template <typename L, bool VEC, int OP>
+mi_status launch_wide(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, const WideState& w,
+                      cudaStream_t st) {
+    constexpr uint32_t W = 256u * (64 / uint32_t(sizeof(L)));
+    const uint32_t tiles_per = (m + W - 1) / W;
+    const uint32_t cap = w.round_tiles < kWideTiles ? w.round_tiles : kWideTiles;
+    if (tiles_per > cap) return set_error(MI_EINVAL, "add: %u limbs exceeds the multi-block maximum", m);
+    const uint32_t per_round = cap / tiles_per;
+    for (uint32_t i0 = 0; i0 < n; i0 += per_round) {
+        const uint32_t k = (n - i0) < per_round ? (n - i0) : per_round;
+        const uint32_t n_tiles = k * tiles_per;
+        MI_CUDA_TRY(cudaMemsetAsync(w.status, 0, size_t(n_tiles) * 4, st));
+        MI_CUDA_TRY(cudaMemsetAsync(w.status + kWideTiles, 0, 4, st));
+        const uint64_t o = uint64_t(i0) * m;
+        k_add_wide<L, VEC, OP><<<n_tiles, 256, 0, st>>>(a + o, b + o, r + o, carry ? carry + i0 : nullptr, m,
+                                                        tiles_per, n_tiles, w.status, w.spin_limit, w.withhold);
+        MI_CUDA_TRY(cudaGetLastError());
+    }
+    return MI_OK;
+}
+
 template <typename L, int Q, int GS, bool VEC, int OP>
 mi_status launch_one(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, cudaStream_t st) {
     constexpr int BLOCK = GS > 256 ? GS : 256;
@@ -257,8 +399,16 @@ uint32_t add_size_class(uint64_t bytes) {
 }
 
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st) {
+                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st, const WideState* wide) {
     const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (limbs % 2 == 0);
+    if (limbs > kAddMaxLimbs64) {
+        if (wide == nullptr || wide->status == nullptr) return set_error(MI_EINVAL, "add: no multi-block state");
+        if (op == ADD_SIX)
+            return vec ? launch_wide<uint64_t, true, ADD_SIX>(a, b, r, nullptr, n, limbs, *wide, st)
+                       : launch_wide<uint64_t, false, ADD_SIX>(a, b, r, nullptr, n, limbs, *wide, st);
+        return vec ? launch_wide<uint64_t, true, ADD_PLAIN>(a, b, r, carry, n, limbs, *wide, st)
+                   : launch_wide<uint64_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, *wide, st);
+    }
     if (op == ADD_SIX) {
         return vec ? dispatch<uint64_t, true, ADD_SIX>(a, b, r, nullptr, n, limbs, thread_bytes, st)
                    : dispatch<uint64_t, false, ADD_SIX>(a, b, r, nullptr, n, limbs, thread_bytes, st);
@@ -268,12 +418,17 @@ mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
 }
 
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st) {
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, const WideState* wide) {
     // An even number of u32 limbs on 8-byte aligned rows is the same bytes as
     // half as many u64 limbs, with the same carry-out.
     if (limbs % 2 == 0 && aligned8(a) && aligned8(b) && aligned8(r))
         return launch_add_u64(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
-                              reinterpret_cast<uint64_t*>(r), carry, n, limbs / 2, ADD_PLAIN, thread_bytes, st);
+                              reinterpret_cast<uint64_t*>(r), carry, n, limbs / 2, ADD_PLAIN, thread_bytes, st,
+                              wide);
+    if (limbs > 2 * kAddMaxLimbs64) {
+        if (wide == nullptr || wide->status == nullptr) return set_error(MI_EINVAL, "add: no multi-block state");
+        return launch_wide<uint32_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, *wide, st);
+    }
     // Odd limb counts (or 4-byte aligned rows) cannot use 128-bit accesses.
     return dispatch<uint32_t, false, ADD_PLAIN>(a, b, r, carry, n, limbs, thread_bytes, st);
 }

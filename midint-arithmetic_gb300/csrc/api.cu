@@ -84,7 +84,7 @@ uint32_t add_bytes(mi_ctx ctx, uint32_t limbs, int limb_bytes) {
 
 mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* carry, uint32_t n, uint32_t limbs,
                   mi_stream stream, int limb_bytes, int op) {
-    const uint32_t maxl = kAddMaxLimbs64 * (8 / limb_bytes);
+    const uint32_t maxl = kAddWideMaxLimbs64 * (8 / limb_bytes);
     MI_TRY(check_batch(a, b, r, limbs, maxl, op == ADD_SIX ? "add6" : "add"));
     const size_t bytes = size_t(n) * limbs * limb_bytes;
     if (partial_overlap(a, bytes, r, bytes) || partial_overlap(b, bytes, r, bytes))
@@ -98,9 +98,9 @@ mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* ca
     const uint32_t tb = add_bytes(ctx, limbs, limb_bytes);
     if (limb_bytes == 8)
         return launch_add_u64(static_cast<const uint64_t*>(a), static_cast<const uint64_t*>(b),
-                              static_cast<uint64_t*>(r), carry, n, limbs, op, tb, st);
+                              static_cast<uint64_t*>(r), carry, n, limbs, op, tb, st, &ctx->wide);
     return launch_add_u32(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
-                          static_cast<uint32_t*>(r), carry, n, limbs, tb, st);
+                          static_cast<uint32_t*>(r), carry, n, limbs, tb, st, &ctx->wide);
 }
 
 mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n, uint32_t limbs, mi_stream stream,
@@ -168,19 +168,31 @@ void* mapped_host(const void* p) {
     return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
 }
 
+// MI_ETIMEOUT (and the error word cleared) when a multi-block addition of the
+// context gave up a bounded wait; call after its stream has been synchronised.
+mi_status wide_status(mi_ctx ctx) {
+    uint32_t err = 0;
+    MI_CUDA_TRY(cudaMemcpy(&err, ctx->wide.status + kWideTiles + 1, 4, cudaMemcpyDeviceToHost));
+    if (err == 0) return MI_OK;
+    MI_CUDA_TRY(cudaMemset(ctx->wide.status + kWideTiles + 1, 0, 4));
+    return set_error(MI_ETIMEOUT, "a multi-block addition gave up waiting for a predecessor tile");
+}
+
 // Runs `launch(da, db, dr, dcarry, count, stream)` over a batch of host
 // buffers, with the tuning of operation class `cls`.  With zero-copy enabled
 // for the class and every buffer mapped pinned memory, one
 // launch reads and writes them in place.  Otherwise the batch is cut into
 // chunks that cycle through kSlots device staging slots: chunk c copies in on
 // the copy-in stream (after the slot's previous copy-out), computes on compute
-// stream c % 2 and copies out on the copy-out stream, so copies in both
+// stream c % 2 (always the first compute stream when `one_compute_stream`: for
+// kernels that share context state between launches) and copies out on the
+// copy-out stream, so copies in both
 // directions and the kernels of neighbouring chunks overlap.
 enum { HOST_ADD = 0, HOST_MUL = 1 };  // operation classes of the host tuning knobs
 
 template <typename F>
 mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, void* h_r, uint8_t* h_carry,
-                        uint32_t n, size_t in_row, size_t out_row, F launch) {
+                        uint32_t n, size_t in_row, size_t out_row, F launch, bool one_compute_stream = false) {
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -209,7 +221,7 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
     for (uint64_t base = 0; base < n; base += chunk, ++c) {
         const uint32_t cnt = uint32_t((n - base) < chunk ? (n - base) : chunk);
         const int slot = c % mi_ctx_s::kSlots;
-        cudaStream_t comp = ctx->pipe[2 + (c & 1)];
+        cudaStream_t comp = ctx->pipe[one_compute_stream ? 2 : 2 + (c & 1)];
         char* stg = static_cast<char*>(ctx->stage[slot]);
         if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
         MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
@@ -276,6 +288,11 @@ mi_status mi_ctx_create(int device, mi_ctx* out) {
             cudaEventCreateWithFlags(&ctx->ev_out[i], cudaEventDisableTiming) != cudaSuccess)
             st = set_error(MI_ECUDA, "mi_ctx_create: event creation failed");
     if (st == MI_OK) st = ntt_tables_create(&ctx->ntt);
+    if (st == MI_OK) {
+        const size_t wb = (size_t(kWideTiles) + 2) * 4;
+        if (cudaMalloc(&ctx->wide.status, wb) != cudaSuccess || cudaMemset(ctx->wide.status, 0, wb) != cudaSuccess)
+            st = set_error(MI_ENOMEM, "mi_ctx_create: multi-block addition state");
+    }
     if (st != MI_OK) {
         mi_ctx_destroy(ctx);
         return st;
@@ -301,6 +318,7 @@ mi_status mi_ctx_destroy(mi_ctx ctx) {
         if (ctx->ev_out[i]) cudaEventDestroy(ctx->ev_out[i]);
     }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->wide.status) cudaFree(ctx->wide.status);
     ntt_tables_destroy(&ctx->ntt);
     delete ctx;
     return MI_OK;
@@ -323,6 +341,12 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
     ctx->ragged_ntt_min = ragged_ntt_min;
     ctx->plain_ntt_min = plain_ntt_min;
     return MI_OK;
+}
+
+mi_status mi_ctx_device_status(mi_ctx ctx) {
+    MI_TRY(check_ctx(ctx));
+    MI_CUDA_TRY(cudaDeviceSynchronize());
+    return wide_status(ctx);
 }
 
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) {
@@ -353,6 +377,19 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             if (value > 1) return set_error(MI_EINVAL, "host zero-copy %u not 0 or 1", value);
             ctx->host_zero_copy[cls] = value;
             return MI_OK;
+        case MI_TUNE_WIDE_SPIN_LIMIT:
+            if (value < 1) return set_error(MI_EINVAL, "spin limit must be at least 1");
+            ctx->wide.spin_limit = value;
+            return MI_OK;
+        case MI_TUNE_WIDE_WITHHOLD:
+            if (value > 1) return set_error(MI_EINVAL, "withhold %u not 0 or 1", value);
+            ctx->wide.withhold = value;
+            return MI_OK;
+        case MI_TUNE_WIDE_ROUND_TILES:
+            if (value < 1 || value > kWideTiles)
+                return set_error(MI_EINVAL, "tiles per round %u outside 1..%u", value, kWideTiles);
+            ctx->wide.round_tiles = value;
+            return MI_OK;
         default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
     }
 }
@@ -371,6 +408,9 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
             if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
             *value = knob == MI_TUNE_HOST_CHUNKS ? ctx->host_chunks[cls] : ctx->host_zero_copy[cls];
             return MI_OK;
+        case MI_TUNE_WIDE_SPIN_LIMIT: *value = ctx->wide.spin_limit; return MI_OK;
+        case MI_TUNE_WIDE_WITHHOLD: *value = ctx->wide.withhold; return MI_OK;
+        case MI_TUNE_WIDE_ROUND_TILES: *value = ctx->wide.round_tiles; return MI_OK;
         default: return set_error(MI_EINVAL, "unknown tuning knob %d", knob);
     }
 }
@@ -436,7 +476,7 @@ mi_status mi_mul_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t*
 mi_status mi_compat_gpuAdd_u64(int num_instances, uint32_t m, const uint64_t* h_as, const uint64_t* h_bs,
                                uint64_t* h_rs) {
     if (num_instances < 0) return set_error(MI_EINVAL, "gpuAdd: negative num_instances");
-    MI_TRY(check_batch(h_as, h_bs, h_rs, m, kAddMaxLimbs64, "gpuAdd"));
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, kAddWideMaxLimbs64, "gpuAdd"));
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     return mi_host_add_u64(ctx, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), m);
@@ -445,16 +485,18 @@ mi_status mi_compat_gpuAdd_u64(int num_instances, uint32_t m, const uint64_t* h_
 mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_as, const uint32_t* h_bs,
                                uint32_t* h_rs) {
     if (num_instances < 0) return set_error(MI_EINVAL, "gpuAdd: negative num_instances");
-    MI_TRY(check_batch(h_as, h_bs, h_rs, m, 2 * kAddMaxLimbs64, "gpuAdd"));
+    MI_TRY(check_batch(h_as, h_bs, h_rs, m, 2 * kAddWideMaxLimbs64, "gpuAdd"));
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 4;
-    return host_pipeline(ctx, HOST_ADD, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [m, tb = add_bytes(ctx, m, 4)](void* da, void* db, void* dr, uint8_t*, uint32_t cnt,
-                                                         cudaStream_t st) {
+    const mi_status st = host_pipeline(ctx, HOST_ADD, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
+                         [ctx, m, tb = add_bytes(ctx, m, 4)](void* da, void* db, void* dr, uint8_t*, uint32_t cnt,
+                                                              cudaStream_t st) {
                              return launch_add_u32(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
-                                                   static_cast<uint32_t*>(dr), nullptr, cnt, m, tb, st);
-                         });
+                                                   static_cast<uint32_t*>(dr), nullptr, cnt, m, tb, st, &ctx->wide);
+                         },
+                         m > 2 * kAddMaxLimbs64);
+    return st == MI_OK && m > 2 * kAddMaxLimbs64 ? wide_status(ctx) : st;
 }
 
 mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_t* h_as, const uint64_t* h_bs,
@@ -583,15 +625,18 @@ mi_status mi_graph_destroy(mi_graph graph) {
 
 mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_r, uint8_t* h_carry,
                           uint32_t n, uint32_t limbs) {
-    MI_TRY(check_batch(h_a, h_b, h_r, limbs, kAddMaxLimbs64, "host_add"));
+    MI_TRY(check_batch(h_a, h_b, h_r, limbs, kAddWideMaxLimbs64, "host_add"));
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
     const size_t row = size_t(limbs) * 8;
-    return host_pipeline(ctx, HOST_ADD, h_a, h_b, h_r, h_carry, n, row, row,
-                         [limbs, tb = add_bytes(ctx, limbs, 8)](void* da, void* db, void* dr, uint8_t* dc,
-                                                                 uint32_t cnt, cudaStream_t st) {
+    const mi_status st = host_pipeline(ctx, HOST_ADD, h_a, h_b, h_r, h_carry, n, row, row,
+                         [ctx, limbs, tb = add_bytes(ctx, limbs, 8)](void* da, void* db, void* dr, uint8_t* dc,
+                                                                      uint32_t cnt, cudaStream_t st) {
                              return launch_add_u64(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
-                                                   static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, tb, st);
-                         });
+                                                   static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, tb, st,
+                                                   &ctx->wide);
+                         },
+                         limbs > kAddMaxLimbs64);
+    return st == MI_OK && limbs > kAddMaxLimbs64 ? wide_status(ctx) : st;
 }
 
 mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_r, uint32_t n,

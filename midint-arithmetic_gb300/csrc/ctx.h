@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "kernels.h"
 #include "ntt_host.h"
 #include "tuning_table.h"
 
@@ -30,6 +31,8 @@ struct mi_ctx_s {
     uint32_t ragged_ntt_min = mi::tuned::kRaggedNttMin;
     // mi_mul_u64: square products of at least this many u64 limbs use the NTT
     uint32_t plain_ntt_min = mi::tuned::kPlainNttMin;
+    // multi-block additions: tile status words, counter and error word
+    mi::WideState wide;
     // addition: operand bytes per thread by size class ceil(log2(u64 limbs))
     uint8_t add_thread_bytes[13] = {};
     mi_ctx_s() {

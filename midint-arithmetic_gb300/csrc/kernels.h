@@ -12,12 +12,27 @@ enum AddOp : int { ADD_PLAIN = 0, ADD_SIX = 1 };
 
 // Batched addition on u64 or u32 limbs (op = ADD_PLAIN or ADD_SIX).
 // Arguments are already validated; n > 0, limbs > 0.
+// Device state of the additions wider than one block (decoupled look-back):
+// `status` holds kWideTiles tile words, then the tile counter, then the error
+// word (set when a bounded wait gave up).  One per context; wide additions on
+// one context must not overlap on the device.
+constexpr uint32_t kWideTiles = 1u << 16;
+struct WideState {
+    uint32_t* status = nullptr;    // kWideTiles + 2 words
+    uint32_t spin_limit = 1u << 20;  // polls of an unpublished predecessor before giving up
+    uint32_t withhold = 0;         // tests only: first tiles never publish (makes the waits run out)
+    uint32_t round_tiles = kWideTiles;  // tiles per launch (at most kWideTiles)
+};
+
 // thread_bytes: operand bytes each thread owns (16, 32 or 64; raised where the
-// instance would need a group of more than 1024 threads).
+// instance would need a group of more than 1024 threads).  Instances wider
+// than one group (limbs above kAddMaxLimbs64 u64 limbs) take the multi-block
+// kernel, which needs `wide`.
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st);
+                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st,
+                         const WideState* wide = nullptr);
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st);
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, const WideState* wide = nullptr);
 // Size class of an addition of `bytes` per operand: ceil(log2(u64 limbs)).
 uint32_t add_size_class(uint64_t bytes);
 
@@ -46,5 +61,7 @@ constexpr uint32_t kMulMaxN32 = 4096;
 // Largest u64 limb count the addition kernels take per instance (one group of
 // at most 1024 threads, 4 limbs each).
 constexpr uint32_t kAddMaxLimbs64 = 4096;
+// Largest u64 limb count of one instance of the multi-block addition.
+constexpr uint32_t kAddWideMaxLimbs64 = 1u << 26;
 
 }  // namespace mi

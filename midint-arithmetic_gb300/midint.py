@@ -33,7 +33,8 @@ RAGGED_NOALLOC_MAX_OPS = 65536
 # Every symbol include/midint.h declares, with (restype, argtypes).
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
 _S = ctypes.c_int  # mi_status
-TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES, TUNE_HOST_CHUNKS, TUNE_HOST_ZERO_COPY = 0, 1, 2, 3, 4
+(TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES, TUNE_HOST_CHUNKS, TUNE_HOST_ZERO_COPY,
+ TUNE_WIDE_SPIN_LIMIT, TUNE_WIDE_WITHHOLD, TUNE_WIDE_ROUND_TILES) = range(8)
 SIGNATURES = {
     "mi_version": (_I, []),
     "mi_status_string": (ctypes.c_char_p, [_I]),
@@ -45,6 +46,7 @@ SIGNATURES = {
     "mi_ctx_set_crossover": (_S, [_P, _U32, _U32]),
     "mi_ctx_set_tuning": (_S, [_P, _I, _U32, _U32]),
     "mi_ctx_get_tuning": (_S, [_P, _I, _U32, _P]),
+    "mi_ctx_device_status": (_S, [_P]),
     "mi_add_u64": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add_u32": (_S, [_P, _P, _P, _P, _P, _U32, _U32, _P]),
     "mi_add6_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
@@ -164,6 +166,11 @@ class Context:
     def set_tuning(self, knob: int, cls: int, value: int) -> None:
         """Overrides one entry of the context's tuning table (TUNE_* knobs)."""
         check(load().mi_ctx_set_tuning(self.handle, knob, cls, value))
+
+    def device_status(self) -> int:
+        """Waits for the device, then MI_OK or MI_ETIMEOUT (a bounded wait of a
+        multi-block addition gave up); the state is cleared by reading it."""
+        return load().mi_ctx_device_status(self.handle)
 
     def get_tuning(self, knob: int, cls: int = 0) -> int:
         v = ctypes.c_uint32()

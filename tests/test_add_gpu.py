@@ -173,7 +173,7 @@ def test_tuning_rejects_bad_values(ctx):
     with pytest.raises(midint.MidintError):
         ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, 130)
     with pytest.raises(midint.MidintError):
-        ctx.set_tuning(7, 0, 1)
+        ctx.set_tuning(99, 0, 1)
     old = ctx.get_tuning(midint.TUNE_PLAIN_NTT_MIN)
     ctx.set_tuning(midint.TUNE_PLAIN_NTT_MIN, 0, 1025)
     assert ctx.get_tuning(midint.TUNE_PLAIN_NTT_MIN) == 1025
