@@ -59,8 +59,8 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
     ap.add_argument("--ragged-ops", type=int, default=200000, help="ops in the ragged batch")
-    ap.add_argument("--sections", default="add,ntt,ragged,serving,u32,fused",
-                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused)")
+    ap.add_argument("--sections", default="add,ntt,ragged,serving,u32,fused,wide",
+                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused, wide)")
     return ap.parse_args()
 
 
@@ -380,6 +380,8 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         res["mul_8192bit_u32limbs"] = u32_section(args, ctx, dev, stream, world, rank)
     if "fused" in sections:
         res["fused"] = fused_section(args, ctx, dev, stream, world, rank)
+    if "wide" in sections:
+        res["wide_add"] = wide_section(args, ctx, dev, stream, world, rank)
     return res
 
 
@@ -482,6 +484,36 @@ def u32_section(args, ctx, dev, stream, world, rank) -> dict:
     del da, db, dr
     torch.cuda.empty_cache()
     return out
+
+
+def wide_section(args, ctx, dev, stream, world, rank) -> dict:
+    """Additions wider than one block: 16 pairs of 2^21 u64 limbs (134 Mbit),
+    multi-block tiles chained by decoupled look-back."""
+    import torch
+
+    import workloads
+
+    sp = stream.cuda_stream
+    hbm = measured_peaks().get("hbm_gbs")
+    n, m = 16, 1 << 21
+    a, b = workloads.add_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 7, rank), worst_every=4)
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(2)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(2)]
+        dr = [torch.empty(a.size, dtype=torch.int64, device=dev) for _ in range(2)]
+        dc = [torch.empty(n, dtype=torch.uint8, device=dev) for _ in range(2)]
+    torch.cuda.synchronize()
+    ms = max_over_ranks(world, time_device(
+        lambda i: ctx.add(da[i], db[i], dr[i], n, m, carry=dc[i], stream=sp), 2, max(10, args.steps // 2),
+        max(args.warmup, 3), stream))
+    status = ctx.device_status()
+    gbs = n * (3 * 8 * m + 1) / (ms * 1e-3) / 1e9
+    del da, db, dr, dc
+    torch.cuda.empty_cache()
+    return {"config": f"{n} pairs x {m} u64 limbs ({64 * m >> 20} Mbit), every 4th pair all-ones + 1 "
+                      "(carries through every tile); 2 rotating sets of 768 MiB",
+            "ms_per_launch": ms, "GB/s": world * gbs, "frac_hbm": (gbs / hbm) if hbm else None,
+            "device_status_ok": status == 0}
 
 
 def fused_section(args, ctx, dev, stream, world, rank) -> dict:

@@ -174,6 +174,31 @@ mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t
                       uint32_t n, uint32_t limbs, mi_stream stream);
 
 /* ---------------------------------------------------------------------------
+ * GMP word formats.  The reference moves every operand through mpz_import /
+ * mpz_export with order -1 and 4-byte native words (cuda/helper.h:116,
+ * 146-170), the same bytes as this library's limbs; these convert batches in
+ * any other mpz_import / mpz_export word format on the device.  A field is
+ * `words` words of `size` bytes (1, 2, 4 or 8) per instance; order 1 = most
+ * significant word first, -1 = least significant first; endian 1 = big-endian
+ * bytes within a word, 0 or -1 = little-endian (native on every supported
+ * host); nails are not supported.
+ * mi_import_words: n fields -> n*limbs u64 limbs (values mod 2^(64*limbs),
+ *   shorter fields zero-extended), like mpz_import per instance.  src aligned
+ *   to `size`.
+ * mi_export_words: n*limbs limbs -> n fixed-width fields: the value's words at
+ *   the least significant end of the field (the start for order -1, the end for
+ *   order 1), zero words elsewhere -- mpz_export's words right- or
+ *   left-aligned in the field; a value wider than the field keeps its low
+ *   words.  counts (nullable) receives mpz_export's count of significant words
+ *   per instance (0 for zero; more than `words` when the value did not fit).
+ * ------------------------------------------------------------------------- */
+mi_status mi_import_words(mi_ctx ctx, const void* src, uint32_t n, uint32_t words, uint32_t size,
+                          int order, int endian, uint64_t* dst, uint32_t limbs, mi_stream stream);
+mi_status mi_export_words(mi_ctx ctx, const uint64_t* src, uint32_t n, uint32_t limbs, void* dst,
+                          uint32_t words, uint32_t size, int order, int endian, uint32_t* counts,
+                          mi_stream stream);
+
+/* ---------------------------------------------------------------------------
  * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 2048: every u64
  * limb is one digit, three 62-bit primes (the first is the reference's
  * FftPrime64, 29*2^57+1) carry the convolution, Garner's CRT and the final

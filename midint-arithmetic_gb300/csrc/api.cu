@@ -459,6 +459,44 @@ mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t
                        reinterpret_cast<uint32_t*>(r), n, 2 * limbs, pick_stream(ctx, stream));
 }
 
+static mi_status check_format(uint32_t words, uint32_t size, int order, int endian, uint32_t limbs, const char* op) {
+    if (words == 0 || limbs == 0) return set_error(MI_EINVAL, "%s: zero words or limbs", op);
+    if (size != 1 && size != 2 && size != 4 && size != 8)
+        return set_error(MI_EINVAL, "%s: word size %u not 1, 2, 4 or 8", op, size);
+    if (order != 1 && order != -1) return set_error(MI_EINVAL, "%s: order %d not 1 or -1", op, order);
+    if (endian < -1 || endian > 1) return set_error(MI_EINVAL, "%s: endian %d not -1, 0 or 1", op, endian);
+    return MI_OK;
+}
+
+mi_status mi_import_words(mi_ctx ctx, const void* src, uint32_t n, uint32_t words, uint32_t size, int order,
+                          int endian, uint64_t* dst, uint32_t limbs, mi_stream stream) {
+    if (src == nullptr || dst == nullptr) return set_error(MI_EINVAL, "import: null buffer");
+    MI_TRY(check_format(words, size, order, endian, limbs, "import"));
+    if ((reinterpret_cast<uintptr_t>(src) % size) != 0 || (reinterpret_cast<uintptr_t>(dst) & 7u) != 0)
+        return set_error(MI_EINVAL, "import: src must be aligned to its word size, dst to 8 bytes");
+    if (n > 0 && any_overlap(src, size_t(n) * words * size, dst, size_t(n) * limbs * 8))
+        return set_error(MI_EINVAL, "import: src and dst overlap");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    return launch_import(src, dst, n, words, size, order, endian, limbs, pick_stream(ctx, stream));
+}
+
+mi_status mi_export_words(mi_ctx ctx, const uint64_t* src, uint32_t n, uint32_t limbs, void* dst, uint32_t words,
+                          uint32_t size, int order, int endian, uint32_t* counts, mi_stream stream) {
+    if (src == nullptr || dst == nullptr) return set_error(MI_EINVAL, "export: null buffer");
+    MI_TRY(check_format(words, size, order, endian, limbs, "export"));
+    if ((reinterpret_cast<uintptr_t>(dst) % size) != 0 || (reinterpret_cast<uintptr_t>(src) & 7u) != 0 ||
+        (reinterpret_cast<uintptr_t>(counts) & 3u) != 0)
+        return set_error(MI_EINVAL, "export: dst must be aligned to its word size, src to 8 bytes, counts to 4");
+    const size_t sb = size_t(n) * limbs * 8, db = size_t(n) * words * size;
+    if (n > 0 && (any_overlap(src, sb, dst, db) || (counts && (any_overlap(counts, size_t(n) * 4, dst, db) ||
+                                                              any_overlap(counts, size_t(n) * 4, src, sb)))))
+        return set_error(MI_EINVAL, "export: buffers overlap");
+    if (n == 0) return MI_OK;
+    MI_TRY(check_ctx(ctx));
+    return launch_export(src, dst, n, limbs, words, size, order, endian, counts, pick_stream(ctx, stream));
+}
+
 mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                          mi_stream stream) {
     return mul_ntt(ctx, a, b, r, n, limbs, stream);

@@ -47,6 +47,13 @@ mi_status launch_mul_lo(const uint32_t* a, const uint32_t* b, uint32_t* r, uint3
 // ((a^2 + b)(b^2 + b) + ab) mod 2^(32*n32) per instance (u32 limb views).
 mi_status launch_poly(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st);
 
+// GMP word-format conversions (convert.cu): fields of `words` words of `size`
+// bytes (1, 2, 4, 8), order 1 / -1, endian 1 (big) / 0, -1 (little).
+mi_status launch_import(const void* src, uint64_t* dst, uint32_t n, uint32_t words, uint32_t size, int order,
+                        int endian, uint32_t limbs, cudaStream_t st);
+mi_status launch_export(const uint64_t* src, void* dst, uint32_t n, uint32_t limbs, uint32_t words, uint32_t size,
+                        int order, int endian, uint32_t* counts, cudaStream_t st);
+
 // Ragged batches (ragged.cu): device scratch words for n_ops, the word that
 // counts skipped ops, the one-time per-device setup (call outside stream
 // capture) and the asynchronous launch sequence.

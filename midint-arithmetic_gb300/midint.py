@@ -63,6 +63,8 @@ SIGNATURES = {
     "mi_calib_mul32_peak": (_S, [_U32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "mi_mul_ntt_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_poly_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
+    "mi_import_words": (_S, [_P, _P, _U32, _U32, _U32, _I, _I, _P, _U32, _P]),
+    "mi_export_words": (_S, [_P, _P, _U32, _U32, _P, _U32, _U32, _I, _I, _P, _P]),
     "mi_mul_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_compat_gpuMulFFT_u16": (_S, [_I, _U32, _P, _P, _P]),
     "mi_ntt_raw": (_S, [ctypes.c_uint64, ctypes.c_uint64, _U32, _U32, _I, _P, _P, _P]),
@@ -209,6 +211,18 @@ class Context:
     def mul_full(self, a, b, r, n: int, limbs: int, limb_bits: int = 64, stream=None) -> None:
         f = load().mi_mul_full_u64 if limb_bits == 64 else load().mi_mul_full_u32
         check(f(self.handle, _ptr(a), _ptr(b), _ptr(r), n, limbs, _ptr(stream)))
+
+    def import_words(self, src, n: int, words: int, size: int, order: int, endian: int, dst, limbs: int,
+                     stream=None) -> None:
+        """GMP word fields (mpz_import conventions) -> u64 limbs, on the device."""
+        check(load().mi_import_words(self.handle, _ptr(src), n, words, size, order, endian, _ptr(dst), limbs,
+                                     _ptr(stream)))
+
+    def export_words(self, src, n: int, limbs: int, dst, words: int, size: int, order: int, endian: int,
+                     counts=None, stream=None) -> None:
+        """u64 limbs -> fixed-width GMP word fields (mpz_export conventions), on the device."""
+        check(load().mi_export_words(self.handle, _ptr(src), n, limbs, _ptr(dst), words, size, order, endian,
+                                     _ptr(counts), _ptr(stream)))
 
     def poly(self, a, b, r, n: int, limbs: int, stream=None) -> None:
         """((a^2 + b)(b^2 + b) + ab) mod 2^(64*limbs), fused (u64 limbs)."""

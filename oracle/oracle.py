@@ -56,6 +56,10 @@ def lib() -> ctypes.CDLL:
         L.orc_gmp_batch.argtypes = [i32, u64, u32, P, P, P, u32, i32]
         L.orc_gmp_batch.restype = i32
         L.orc_batch_u64.argtypes = [i32, u64, u32, P, P, P, P, i32]
+        L.orc_gmp_import.argtypes = [P, u32, i32, u32, i32, P, u32]
+        L.orc_gmp_import.restype = i32
+        L.orc_gmp_export.argtypes = [P, u32, i32, u32, i32, P, u32]
+        L.orc_gmp_export.restype = i32
         _lib = L
     return _lib
 
@@ -165,6 +169,66 @@ def batch_u64(op: str, a: np.ndarray, b: np.ndarray, m: int, threads: int = 1):
     r = np.empty(n * 2 * m, np.uint64)
     lib().orc_batch_u64(1, n, m, _p(a), _p(b), _p(r), None, threads)
     return r
+
+
+# --- word formats (GMP mpz_import / mpz_export conventions) ----------------------
+#
+# A field of `words` words of `size` bytes per instance; `order` 1 = most
+# significant word first, -1 = least significant first; `endian` 1 = big-endian
+# bytes in a word, -1 or 0 = little-endian (native on every supported host).
+# These restate GMP's documented formats; test_oracle.py pins them on GMP itself.
+
+def import_words(src: np.ndarray, n: int, words: int, size: int, order: int, endian: int,
+                 limbs: int) -> np.ndarray:
+    """Fields of GMP words -> n*limbs u64 limbs (values mod 2^(64*limbs))."""
+    b = np.ascontiguousarray(src).view(np.uint8).reshape(n, words, size)
+    if order == 1:
+        b = b[:, ::-1, :]
+    if endian == 1:
+        b = b[:, :, ::-1]
+    le = np.ascontiguousarray(b).reshape(n, words * size)      # little-endian bytes of each value
+    out = np.zeros((n, limbs * 8), np.uint8)
+    k = min(limbs * 8, words * size)
+    out[:, :k] = le[:, :k]
+    return out.view(np.uint64).ravel()
+
+
+def export_words(src: np.ndarray, n: int, limbs: int, words: int, size: int, order: int, endian: int):
+    """n*limbs u64 limbs -> (fields of GMP words as uint8, significant-word counts).
+    Values wider than the field keep their low words (the counts say so)."""
+    le = np.ascontiguousarray(src, dtype=np.uint64).reshape(n, limbs).view(np.uint8).reshape(n, limbs * 8)
+    field = np.zeros((n, words * size), np.uint8)
+    k = min(limbs * 8, words * size)
+    field[:, :k] = le[:, :k]
+    nz = le != 0
+    top = np.where(nz.any(axis=1), limbs * 8 - 1 - np.argmax(nz[:, ::-1], axis=1), -1)
+    counts = np.where(top >= 0, top // size + 1, 0).astype(np.uint32)
+    b = field.reshape(n, words, size)
+    if endian == 1:
+        b = b[:, :, ::-1]
+    if order == 1:
+        b = b[:, ::-1, :]
+    return np.ascontiguousarray(b).ravel(), counts
+
+
+def gmp_import(src_field: np.ndarray, words: int, size: int, order: int, endian: int, limbs: int):
+    """GMP's mpz_import of one field -> (limbs u64, significant limbs)."""
+    f = np.ascontiguousarray(src_field, dtype=np.uint8)
+    out = np.zeros(limbs, np.uint64)
+    cnt = lib().orc_gmp_import(_p(f), words, order, size, endian, _p(out), limbs)
+    if cnt < 0:
+        raise RuntimeError("GMP (libgmp.so.10) not available")
+    return out, cnt
+
+
+def gmp_export(x: np.ndarray, words: int, size: int, order: int, endian: int):
+    """GMP's mpz_export of one value into a field of `words` words -> (field, count)."""
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    field = np.zeros(words * size, np.uint8)
+    cnt = lib().orc_gmp_export(_p(x), x.size, order, size, endian, _p(field), words)
+    if cnt < 0:
+        raise RuntimeError("GMP (libgmp.so.10) not available")
+    return field, cnt
 
 
 # --- pure-Python int cross-oracles (small cases) --------------------------------

@@ -10,6 +10,9 @@
  *   orc_zmod_*, orc_ntt_*  prime-field NTT      cuda/ker-fft-mul.cu.h:76-140,191-211,304-368
  *   orc_gmp_*     the reference CPU path gmpAddMulOnce over GMP
  *                                               cuda/helper.h:146-170, cuda/main.cu:165-175,358-368
+ *   orc_gmp_import / orc_gmp_export  GMP's own mpz_import / mpz_export, the
+ *                 word formats the reference's conversions use (cuda/helper.h:116,
+ *                 146-170), to pin the import/export restatement in oracle.py
  * Limb layout everywhere: instance i at [i*m, (i+1)*m), limb 0 least
  * significant (cuda/helper.h:116, GMP_ORDER -1).
  *
@@ -441,4 +444,54 @@ void orc_batch_u64(int op, uint64_t n, uint32_t m, const uint64_t* a, const uint
         for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
     free(th);
     free(jobs);
+}
+
+/* ------------------------------------------------------------------------
+ * GMP's own word-format conversions (mpz_import / mpz_export with any
+ * order, word size and byte order), to pin the restatement in oracle.py.
+ * ---------------------------------------------------------------------- */
+
+/* `count` words of `size` bytes at src (GMP's order / endian conventions) ->
+ * `nlimbs` u64 limbs, least significant first, zero filled (higher limbs
+ * dropped).  Returns the number of significant limbs, or -1 without GMP. */
+int orc_gmp_import(const void* src, uint32_t count, int order, uint32_t size, int endian, uint64_t* limbs,
+                   uint32_t nlimbs) {
+    if (!orc_gmp_available()) return -1;
+    orc_mpz z;
+    G.init(&z);
+    G.import_(&z, count, order, size, endian, 0, src);
+    uint64_t* buf = (uint64_t*)calloc((size_t)count * size / 8 + 2, 8);
+    size_t cnt = 0;
+    G.export_(buf, &cnt, -1, 8, 0, 0, &z);
+    for (uint32_t j = 0; j < nlimbs; ++j) limbs[j] = j < cnt ? buf[j] : 0;
+    free(buf);
+    G.clear(&z);
+    return (int)cnt;
+}
+
+/* `nlimbs` u64 limbs -> mpz_export with (order, size, endian) into a
+ * fixed-width field of `words` words: GMP's `count` significant words, placed
+ * at the least significant end of the field (the start for order -1, the end
+ * for order 1), the rest zero.  Returns count (count > words: did not fit and
+ * nothing is written), or -1 without GMP. */
+int orc_gmp_export(const uint64_t* limbs, uint32_t nlimbs, int order, uint32_t size, int endian, void* dst,
+                   uint32_t words) {
+    if (!orc_gmp_available()) return -1;
+    orc_mpz z;
+    G.init(&z);
+    G.import_(&z, nlimbs, -1, 8, 0, 0, limbs);
+    uint8_t* buf = (uint8_t*)calloc((size_t)nlimbs * 8 / size + 2, size);
+    size_t cnt = 0;
+    G.export_(buf, &cnt, order, size, endian, 0, &z);
+    G.clear(&z);
+    if (cnt <= words) {
+        uint8_t* d = (uint8_t*)dst;
+        memset(d, 0, (size_t)words * size);
+        if (order < 0)
+            memcpy(d, buf, cnt * size);
+        else
+            memcpy(d + (size_t)(words - cnt) * size, buf, cnt * size);
+    }
+    free(buf);
+    return (int)cnt;
 }

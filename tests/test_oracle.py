@@ -149,3 +149,40 @@ def test_workload_generators_are_deterministic():
     assert (b.reshape(16, 4)[::8, 0] == 1).all() and not b.reshape(16, 4)[::8, 1:].any()
     a2, _ = W.add_pairs(n=16, m=4)
     assert np.array_equal(a, a2)
+
+
+FORMATS = [(order, size, endian) for order in (-1, 1) for size in (1, 2, 4, 8) for endian in (-1, 0, 1)]
+
+
+@pytest.mark.parametrize("order,size,endian", FORMATS)
+def test_word_formats_match_gmp(order, size, endian):
+    """The import/export restatement against GMP's own mpz_import/mpz_export."""
+    if not O.gmp_available():
+        pytest.skip("libgmp.so.10 not present")
+    rng = np.random.default_rng(size * 7 + order + endian)
+    limbs = 5
+    for words in (1, 3, 40 // size, 40 // size + 3):
+        n = 4
+        x = rng.integers(0, 2**64, size=n * limbs, dtype=np.uint64)
+        x[limbs:2 * limbs] = 0                             # a zero value
+        x[2 * limbs + 2:3 * limbs] = 0                     # a short value
+        field, counts = O.export_words(x, n, limbs, words, size, order, endian)
+        back = O.import_words(field, n, words, size, order, endian, limbs)
+        for i in range(n):
+            xi = x[i * limbs:(i + 1) * limbs]
+            f, cnt = O.gmp_export(xi, words, size, order, endian)
+            assert cnt == counts[i]
+            if cnt <= words:
+                assert np.array_equal(f, field[i * words * size:(i + 1) * words * size])
+                assert np.array_equal(back[i * limbs:(i + 1) * limbs], xi)
+            g, _ = O.gmp_import(field[i * words * size:(i + 1) * words * size], words, size, order, endian, limbs)
+            assert np.array_equal(g, back[i * limbs:(i + 1) * limbs])
+
+
+def test_reference_word_format_is_u32_least_first():
+    # cuda/helper.h:116-170 imports and exports order -1, 4-byte native words:
+    # the same bytes as the library's u64 limbs
+    rng = np.random.default_rng(1)
+    x = rng.integers(0, 2**64, size=3 * 4, dtype=np.uint64)
+    field, _ = O.export_words(x, 3, 4, 8, 4, -1, 0)
+    assert np.array_equal(field.view(np.uint64), x)
