@@ -1,0 +1,216 @@
+// ntt32.cuh -- 30-bit prime fields and the shared-memory NTT of the
+// multiplication kernels.
+//
+// Field: p < 2^30 with 2^21 | p - 1; residues kept lazily in [0, 2p), so every
+// sum and difference of two residues fits 32 bits.  Twiddle products use
+// Shoup's method with a precomputed companion w' = floor(w * 2^32 / p):
+// x*w mod p = x*w - hi(x*w')*p in [0, 2p) for any 32-bit x, three integer
+// multiplies.  Products of two variables (the pointwise product of spectra)
+// use Montgomery reduction with R = 2^32 (four multiplies), whose 1/R is folded
+// into one operand's conversion.  These replace zmod_t
+// (cuda/ker-fft-mul.cu.h:76-140), whose multiply is a `%` on the double-width
+// product.
+//
+// Transform: length L = 2^LG held by L/8 threads, 8 residues each, in
+// registers.  The forward transform is decimation in frequency (natural order
+// in, bit-reversed out) done as radix-8 passes (three butterfly stages in
+// registers) at strides L/8, L/64, ... and one final radix-2 or radix-4 pass
+// on 8 consecutive residues; the inverse is decimation in time in the reverse
+// pass order (bit-reversed in, natural out).  Between passes the residues are
+// exchanged through shared memory with an XOR swizzle of 32-bit words that
+// keeps the passes free of bank conflicts (one 2-way exchange at L = 1024).
+// The reference instead runs lg L radix-2 stages in shared memory with a
+// barrier per stage, after a bit-reversal permutation with a barrier per
+// element, and reads each twiddle from global memory (fft/ifft,
+// cuda/ker-fft-mul.cu.h:304-368).
+//
+// Twiddles: tw[e] = (w^e, floor(w^e 2^32 / p)) and itw[e] the same for w^-e,
+// e < 2048, w a primitive 4096th root of unity; a length-L transform reads
+// every (4096/L)-th entry.
+#pragma once
+
+#include <cstdint>
+
+namespace mi {
+namespace ntt32 {
+
+constexpr int kLgMax = 12;                     // 4096-point transforms at most
+constexpr int kTwiddles = (1 << kLgMax) / 2;   // entries per table
+constexpr int kPrimes = 5;
+
+struct Field {
+    uint32_t p, p2, pinv;  // pinv = -p^-1 mod 2^32
+    __device__ __forceinline__ uint32_t add(uint32_t u, uint32_t v) const {
+        const uint32_t s = u + v;  // < 4p
+        return min(s, s - p2);
+    }
+    // u - v + 2p in (0, 4p), reduced to [0, 2p)
+    __device__ __forceinline__ uint32_t sub(uint32_t u, uint32_t v) const {
+        const uint32_t s = u + p2 - v;
+        return min(s, s - p2);
+    }
+    __device__ __forceinline__ uint32_t shoup(uint32_t x, uint2 w) const {
+        const uint32_t q = __umulhi(x, w.y);
+        return x * w.x - q * p;
+    }
+    // x*y/2^32 mod p in [0, 2p) for x, y < 2p
+    __device__ __forceinline__ uint32_t mont(uint32_t x, uint32_t y) const {
+        const uint32_t lo = x * y, hi = __umulhi(x, y);
+        const uint32_t m = lo * pinv;
+        return hi + __umulhi(m, p) + (lo != 0u ? 1u : 0u);
+    }
+    __device__ __forceinline__ uint32_t reduce(uint32_t x) const { return min(x, x - p); }
+};
+
+// Shared-memory word of residue index i: XOR of bits 2-4 with bits 5-7.  A
+// bijection inside every 256-word block that keeps aligned quads together
+// (so the consecutive layout moves four residues per access).
+__device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ (((i >> 5) & 7u) << 2); }
+
+template <int LG>
+struct Plan {
+    static constexpr int L = 1 << LG;
+    static constexpr int NT = L / 8;             // threads per transform
+    static constexpr int NF = LG / 3;            // radix-8 passes
+    static constexpr int R = LG - 3 * NF;        // stages left for the final pass
+    static constexpr int S = (1 << kLgMax) / L;  // twiddle-table stride
+    __host__ __device__ static constexpr int d(int k) { return k < NF ? (L >> (3 * (k + 1))) : 1; }
+    __device__ static __forceinline__ uint32_t idx(int d, uint32_t t, int j) {
+        return (t / d) * 8 * d + (t % d) + d * j;
+    }
+};
+
+// Moves the thread's 8 residues from layout (stride) d_from to d_to through
+// shared memory; the second barrier protects `sh` for the next exchange.
+template <int LG>
+__device__ __forceinline__ void exchange(uint32_t (&x)[8], uint32_t* sh, int d_from, int d_to) {
+    using P = Plan<LG>;
+    const uint32_t t = threadIdx.x % P::NT;
+    if (d_from == 1) {
+#pragma unroll
+        for (int j = 0; j < 8; j += 4)
+            *reinterpret_cast<uint4*>(sh + swz(P::idx(1, t, j))) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sh[swz(P::idx(d_from, t, j))] = x[j];
+    }
+    __syncthreads();
+    if (d_to == 1) {
+#pragma unroll
+        for (int j = 0; j < 8; j += 4) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sh + swz(P::idx(1, t, j)));
+            x[j] = v.x;
+            x[j + 1] = v.y;
+            x[j + 2] = v.z;
+            x[j + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = sh[swz(P::idx(d_to, t, j))];
+    }
+    __syncthreads();
+}
+
+// Forward transform (DIF).  In: x[j] = residue t + L/8*j (natural order),
+// values in [0, 2p).  Out: layout stride 1 (x[j] = slot 8t+j of the
+// bit-reversed spectrum), values in [0, 2p).
+template <int LG>
+__device__ __forceinline__ void forward(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ tw, const Field& f) {
+    using P = Plan<LG>;
+    const uint32_t t = threadIdx.x % P::NT;
+    auto bf = [&](int j, int k, uint32_t e) {
+        const uint32_t u = x[j], v = x[k];
+        x[j] = f.add(u, v);
+        x[k] = f.shoup(u + f.p2 - v, __ldg(tw + e));
+    };
+#pragma unroll
+    for (int k = 0; k < P::NF; ++k) {
+        const int d = P::d(k);
+        if (k > 0) exchange<LG>(x, sh, P::d(k - 1), d);
+        const uint32_t off = t % d;
+        const uint32_t mult = uint32_t(P::S) << (3 * k);  // (L / 8d) * S
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bf(j, j + 4, (off + d * j) * mult);
+#pragma unroll
+        for (int j = 0; j < 8; j += 4) {
+            bf(j, j + 2, off * 2 * mult);
+            bf(j + 1, j + 3, (off + d) * 2 * mult);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) bf(j, j + 1, off * 4 * mult);
+    }
+    if constexpr (P::R > 0) {
+        exchange<LG>(x, sh, P::d(P::NF - 1), 1);
+        if constexpr (P::R == 2) {
+            const uint2 w1 = __ldg(tw + uint32_t(P::L / 4) * P::S);
+#pragma unroll
+            for (int j = 0; j < 8; j += 4) {
+                const uint32_t u0 = x[j], v0 = x[j + 2], u1 = x[j + 1], v1 = x[j + 3];
+                x[j] = f.add(u0, v0);
+                x[j + 2] = f.sub(u0, v0);  // twiddle 1
+                x[j + 1] = f.add(u1, v1);
+                x[j + 3] = f.shoup(u1 + f.p2 - v1, w1);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {  // twiddle 1
+            const uint32_t u = x[j], v = x[j + 1];
+            x[j] = f.add(u, v);
+            x[j + 1] = f.sub(u, v);
+        }
+    }
+}
+
+// Inverse transform without the 1/L scaling (DIT).  In: stride-1 layout of a
+// bit-reversed spectrum; out: x[j] = residue t + L/8*j in natural order;
+// values in [0, 2p) throughout.
+template <int LG>
+__device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ itw,
+                                        const Field& f) {
+    using P = Plan<LG>;
+    const uint32_t t = threadIdx.x % P::NT;
+    auto bf = [&](int j, int k, uint32_t e) {
+        const uint32_t u = x[j], v = f.shoup(x[k], __ldg(itw + e));
+        x[j] = f.add(u, v);
+        x[k] = f.sub(u, v);
+    };
+    if constexpr (P::R > 0) {
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {  // twiddle 1
+            const uint32_t u = x[j], v = x[j + 1];
+            x[j] = f.add(u, v);
+            x[j + 1] = f.sub(u, v);
+        }
+        if constexpr (P::R == 2) {
+            const uint2 w1 = __ldg(itw + uint32_t(P::L / 4) * P::S);
+#pragma unroll
+            for (int j = 0; j < 8; j += 4) {
+                const uint32_t u0 = x[j], v0 = x[j + 2], u1 = x[j + 1], v1 = f.shoup(x[j + 3], w1);
+                x[j] = f.add(u0, v0);
+                x[j + 2] = f.sub(u0, v0);
+                x[j + 1] = f.add(u1, v1);
+                x[j + 3] = f.sub(u1, v1);
+            }
+        }
+        exchange<LG>(x, sh, 1, P::d(P::NF - 1));
+    }
+#pragma unroll
+    for (int k = P::NF - 1; k >= 0; --k) {
+        const int d = P::d(k);
+        const uint32_t off = t % d;
+        const uint32_t mult = uint32_t(P::S) << (3 * k);
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) bf(j, j + 1, off * 4 * mult);
+#pragma unroll
+        for (int j = 0; j < 8; j += 4) {
+            bf(j, j + 2, off * 2 * mult);
+            bf(j + 1, j + 3, (off + d) * 2 * mult);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bf(j, j + 4, (off + d * j) * mult);
+        if (k > 0) exchange<LG>(x, sh, d, P::d(k - 1));
+    }
+}
+
+}  // namespace ntt32
+}  // namespace mi

@@ -5,13 +5,16 @@
 //
 // The reference rebuilds and copies its twiddle tables on every driver call
 // (getOmega / mkOmegas, cuda/ker-fft-mul.cu.h:191-211; cuda/main.cu:458-470);
-// here they are built once per context and stay in device memory.
+// here they are built once per context and stay in device memory: for each of
+// the five 30-bit primes of the multiplication kernels, w^e and w^-e with
+// their Shoup companions (w = g^((p-1)/4096), the getOmega convention).
 #include <cstring>
 #include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
 #include "ntt.cuh"
+#include "ntt32.cuh"
 #include "ntt_host.h"
 
 namespace mi {
@@ -47,30 +50,47 @@ void host_twiddles(uint64_t p, uint64_t g, uint32_t s, uint64_t* tw, uint64_t* i
     }
 }
 
+static uint2 shoup_pair(uint64_t c, uint32_t p) {
+    c %= p;
+    return make_uint2(uint32_t(c), uint32_t((c << 32) / p));
+}
+
 mi_status ntt_tables_create(NttTables* T) {
-    constexpr int E = ntt::kTwiddles;
-    std::vector<uint64_t> h(size_t(6) * E);
+    constexpr int E = ntt32::kTwiddles;
+    std::vector<uint2> h(size_t(10) * E);
     NttMulParams& P = T->params;
     std::memset(&P, 0, sizeof(P));
-    for (int q = 0; q < 3; ++q) {
-        const uint64_t p = kNttPrimes[q].p;
-        host_twiddles(p, kNttPrimes[q].g, kNttPrimes[q].s, &h[size_t(2 * q) * E], &h[size_t(2 * q + 1) * E]);
+    for (int q = 0; q < 5; ++q) {
+        const uint32_t p = kNttPrimes[q].p;
+        const uint64_t w = host_powmod(kNttPrimes[q].g, (uint64_t(p) - 1) >> ntt32::kLgMax, p);  // order 4096
+        const uint64_t wi = host_invmod(w, p);
+        uint64_t acc = 1, acci = 1;
+        for (int e = 0; e < E; ++e) {
+            h[size_t(2 * q) * E + e] = shoup_pair(acc, p);
+            h[size_t(2 * q + 1) * E + e] = shoup_pair(acci, p);
+            acc = host_mulmod(acc, w, p);
+            acci = host_mulmod(acci, wi, p);
+        }
         P.p[q] = p;
-        P.c[q] = uint32_t(p >> 32);
-        const uint64_t R = r_mod(p);
-        P.kb[q] = host_mulmod(R, R, p);
-        for (int lg = 0; lg <= ntt::kLgMax; ++lg) P.ka_by_lg[q][lg] = host_mulmod(R, host_invmod(uint64_t(1) << lg, p), p);
+        uint32_t inv = 1;  // p^-1 mod 2^32 by Newton iteration
+        for (int i = 0; i < 5; ++i) inv *= 2 - p * inv;
+        P.pinv[q] = 0u - inv;
+        const uint64_t r32 = (uint64_t(1) << 32) % p, r64 = host_mulmod(r32, r32, p);
+        for (int lg = 8; lg <= ntt32::kLgMax; ++lg) {
+            const uint64_t li = host_invmod(uint64_t(1) << lg, p);
+            P.ka_by_lg[q][lg - 8][0] = shoup_pair(li, p);
+            P.ka_by_lg[q][lg - 8][1] = shoup_pair(host_mulmod(li, r32, p), p);
+        }
+        P.kb[q][0] = shoup_pair(r32, p);
+        P.kb[q][1] = shoup_pair(r64, p);
     }
-    const uint64_t q0 = kNttPrimes[0].p, q1 = kNttPrimes[1].p, q2 = kNttPrimes[2].p;
-    P.g01 = host_mulmod(host_invmod(q0 % q1, q1), r_mod(q1), q1);
-    P.g02 = host_mulmod(host_invmod(q0 % q2, q2), r_mod(q2), q2);
-    P.g12 = host_mulmod(host_invmod(q1 % q2, q2), r_mod(q2), q2);
-    const u128 q01 = (u128)q0 * q1;
-    P.q01_lo = uint64_t(q01);
-    P.q01_hi = uint64_t(q01 >> 64);
-    MI_CUDA_TRY(cudaMalloc(&T->d_tw, h.size() * sizeof(uint64_t)));
-    MI_CUDA_TRY(cudaMemcpy(T->d_tw, h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
-    for (int q = 0; q < 3; ++q) {
+    int c = 0;
+    for (int i = 1; i < 5; ++i)
+        for (int k = 0; k < i; ++k)
+            P.garner[c++] = shoup_pair(host_invmod(kNttPrimes[k].p % kNttPrimes[i].p, kNttPrimes[i].p), kNttPrimes[i].p);
+    MI_CUDA_TRY(cudaMalloc(&T->d_tw, h.size() * sizeof(uint2)));
+    MI_CUDA_TRY(cudaMemcpy(T->d_tw, h.data(), h.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    for (int q = 0; q < 5; ++q) {
         P.tw[q] = T->d_tw + size_t(2 * q) * E;
         P.itw[q] = T->d_tw + size_t(2 * q + 1) * E;
     }

@@ -10,37 +10,31 @@ namespace mi {
 
 constexpr uint32_t kNttMaxLimbs = 2048;  // u64 limbs per operand (4096-point transforms)
 
-// One NTT prime: p = c*2^32 + 1 < 2^62, g of multiplicative order exactly 2^s
-// (the reference's FftPrime convention, cuda/ker-fft-mul.cu.h:44-72).
-struct NttPrime {
-    uint64_t p;
-    uint64_t g;
-    uint32_t s;
+// The five primes of the multiplication kernels: p < 2^30, 2^21 | p - 1, g a
+// primitive root (product 2^149.4 > 2048 * 2^128, the largest coefficient).
+struct NttPrime30 {
+    uint32_t p;
+    uint32_t g;
+};
+constexpr NttPrime30 kNttPrimes[5] = {
+    {1012924417u, 5u}, {1004535809u, 3u}, {998244353u, 3u}, {985661441u, 3u}, {975175681u, 17u},
 };
 
-// q0 < q1 < q2.  q0 is the reference's FftPrime64 (29*2^57+1, g = 21, s = 57).
-constexpr NttPrime kNttPrimes[3] = {
-    {4179340454199820289ull, 21ull, 57},
-    {4611685692009873409ull, 3173265456634446468ull, 34},
-    {4611685941117976577ull, 391383840822949112ull, 33},
-};
-
-// Kernel parameter block (passed by value).
+// Kernel parameter block (passed by value).  Constants with a Shoup
+// companion are (c, floor(c 2^32 / p)) pairs.
 struct NttMulParams {
-    uint64_t p[3];
-    uint32_t c[3];
-    uint64_t ka[3];            // R/L mod p for the launch's transform length
-    uint64_t kb[3];            // R^2 mod p
-    uint64_t ka_by_lg[3][13];  // R/2^lg mod p, lg <= 12
-    const uint64_t* tw[3];     // w^e R mod p, e < 2048
-    const uint64_t* itw[3];    // w^-e R mod p
-    uint64_t g01, g02, g12;    // Garner constants q0^-1 mod q1, q0^-1 mod q2, q1^-1 mod q2 (times R)
-    uint64_t q01_lo, q01_hi;   // q0*q1
+    uint32_t p[5];
+    uint32_t pinv[5];             // -p^-1 mod 2^32
+    uint2 ka_by_lg[5][5][2];      // a's conversion for L = 2^(8+i): (L^-1, 2^32 L^-1) mod p
+    uint2 kb[5][2];               // b's conversion: (2^32, 2^64) mod p
+    uint2 garner[10];             // p_k^-1 mod p_i, for i = 1..4, k = 0..i-1
+    const uint2* tw[5];           // (w^e, companion), e < 2048, w of order 4096
+    const uint2* itw[5];          // (w^-e, companion)
 };
 
-// Device-resident tables of one context (96 KiB) and the parameter block.
+// Device-resident tables of one context (160 KiB) and the parameter block.
 struct NttTables {
-    uint64_t* d_tw = nullptr;
+    uint2* d_tw = nullptr;
     NttMulParams params{};
 };
 
@@ -68,7 +62,9 @@ struct NttRawArgs {
 };
 mi_status launch_ntt_raw(const NttRawArgs& A, cudaStream_t st);
 
-// Host modular arithmetic (exact, 128-bit intermediates).
+// Host modular arithmetic (exact, 128-bit intermediates).  The raw transform
+// path (mi_ntt_raw) keeps 64-bit fields so it can run the reference's own
+// primes.
 uint64_t host_mulmod(uint64_t a, uint64_t b, uint64_t p);
 uint64_t host_powmod(uint64_t a, uint64_t e, uint64_t p);
 uint64_t host_invmod(uint64_t a, uint64_t p);  // p prime

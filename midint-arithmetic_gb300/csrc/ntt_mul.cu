@@ -6,23 +6,25 @@
 // prime from 16 digits on, and cuda/main.cu:729-739 disables validation).
 //
 // Here every u64 limb is one digit; the product of two m-limb integers has
-// coefficients below m * 2^128 <= 2^139 (m <= 2048), so three primes
-// q0 < q1 < q2 < 2^62 (product 2^186) recover every coefficient exactly by
-// CRT.  One CTA of L/8 threads owns one instance (L = pow2ceil(2m) >= 256):
-// for each prime it converts a and b into the field (a scaled by 1/L, so the
-// inverse transform needs no scaling pass), runs two forward transforms,
-// multiplies pointwise and runs the inverse transform (ntt.cuh), leaving the
-// residues in shared memory.  The same CTA then recombines each coefficient
-// with Garner's formula, sums the three-word coefficients of its 8 output
-// limbs, passes the overflow words to its right neighbour and resolves the
-// remaining one-bit carries with mi::group_carry -- the final carry that the
-// reference does with splitFftReg + baddRegMul2Fft.
+// coefficients below m * 2^128 <= 2^139 (m <= 2048), so five primes
+// p_i < 2^30 (product 2^149.4) recover every coefficient exactly by CRT.  One
+// CTA of L/8 threads owns one instance (L = pow2ceil(2m) >= 256): for each
+// prime it converts a and b into the field, runs two forward transforms,
+// multiplies pointwise and runs the inverse transform (ntt32.cuh), leaving
+// the residues in shared memory.  The same CTA then recombines each
+// coefficient with Garner's formula, sums the three-word coefficients of its
+// 8 output limbs, passes the overflow words to its right neighbour and
+// resolves the remaining one-bit carries with mi::group_carry -- the final
+// carry that the reference does with splitFftReg + baddRegMul2Fft.
+// (ntt_raw below keeps the 64-bit fields of ntt.cuh, so it can run the
+// reference's own primes on its known answers.)
 #include <cstdio>
 
 #include "common.cuh"
 #include "kernels.h"
 #include "ntt.cuh"
 #include "ntt_host.h"
+#include "ntt32.cuh"
 #include "ntt_mul.cuh"
 
 namespace mi {
@@ -36,7 +38,7 @@ template <int LG>
 struct NttShape {
     static constexpr int L = 1 << LG;
     static constexpr int NT = L / 8;
-    static constexpr size_t SMEM = ntt::MulSmem<LG>::WORDS64 * 8 + size_t(NT / 32 + 1) * 4;
+    static constexpr size_t SMEM = ntt32::MulSmem<LG>::WORDS32 * 4 + size_t(NT / 32 + 1) * 4;
 };
 
 // 768 threads per SM: three 256-thread CTAs for 2048-point transforms (one
@@ -45,10 +47,10 @@ template <int LG>
 __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     k_ntt_mul(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ r, uint32_t n,
               uint32_t m, uint32_t rlen, NttMulParams P) {
-    extern __shared__ __align__(16) uint64_t smem[];
-    uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + ntt::MulSmem<LG>::WORDS64);
+    extern __shared__ __align__(16) uint32_t smem32[];
+    uint32_t* scratch = smem32 + ntt32::MulSmem<LG>::WORDS32;
     for (uint64_t inst = blockIdx.x; inst < n; inst += gridDim.x)
-        ntt::mul_one<LG>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem, scratch);
+        ntt32::mul_one<LG>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
 }
 
 template <int LG>
@@ -115,8 +117,7 @@ mi_status launch_mul_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
     const uint32_t rlen = low ? m : 2 * m;
     uint32_t L = pow2ceil(2 * m);
     if (L < 256) L = 256;
-    NttMulParams P = base;
-    for (int q = 0; q < 3; ++q) P.ka[q] = base.ka_by_lg[q][__builtin_ctz(L)];
+    const NttMulParams& P = base;
     switch (L) {
         case 256: return launch_lg<8>(a, b, r, n, m, rlen, P, st);
         case 512: return launch_lg<9>(a, b, r, n, m, rlen, P, st);

@@ -3,121 +3,153 @@
 //
 // Every u64 limb is one digit; the product of an la-limb and an lb-limb
 // integer has coefficients below min(la, lb) * 2^128 <= 2^139 (limbs <= 2048),
-// so three primes q0 < q1 < q2 < 2^62 (product 2^186) recover every coefficient
+// so five primes p_i < 2^30 (product 2^149.4) recover every coefficient
 // exactly by CRT.  For each prime the group converts a and b into the field
-// (a scaled by 1/L, so the inverse transform needs no scaling pass), runs two
+// (a scaled by 1/L, so the inverse transform needs no scaling pass, and b by
+// 2^32, which the Montgomery pointwise product takes out again), runs two
 // forward transforms, multiplies pointwise and runs the inverse transform
-// (ntt.cuh), leaving the residues in shared memory.  It then recombines each
-// coefficient with Garner's formula, sums the three-word coefficients of its 8
-// output limbs, passes the overflow words to its right neighbour and resolves
-// the remaining one-bit carries with mi::group_carry -- the final carry that
-// the reference does with splitFftReg + baddRegMul2Fft
-// (cuda/ker-fft-help.cu.h:3-95).
+// (ntt32.cuh), leaving the residues in shared memory.  It then recombines each
+// coefficient with Garner's mixed-radix formula (ten Shoup products by
+// constant inverses, then a Horner evaluation in 32-bit words), sums the
+// three-word coefficients of its 8 output limbs, passes the overflow words to
+// its right neighbour and resolves the remaining one-bit carries with
+// mi::group_carry -- the final carry that the reference does with
+// splitFftReg + baddRegMul2Fft (cuda/ker-fft-help.cu.h:3-95).
 #pragma once
 
 #include "common.cuh"
-#include "ntt.cuh"
+#include "ntt32.cuh"
 #include "ntt_host.h"
 
 namespace mi {
-namespace ntt {
+namespace ntt32 {
 
-// Shared memory of one group: exchange buffer (L) + three residue arrays (3L).
+// Shared memory of one group, in 32-bit words: exchange buffer (L) + five
+// residue arrays (5L); a's spectrum waits in the last residue array.
 template <int LG>
 struct MulSmem {
     static constexpr int L = 1 << LG;
-    static constexpr size_t WORDS64 = size_t(4) * L;
+    static constexpr size_t WORDS32 = size_t(6) * L;
 };
+
+// x*K mod p in [0, 2p) for a 64-bit digit x: K0 = K mod p, K1 = 2^32 K mod p
+// (Shoup pairs).
+__device__ __forceinline__ uint32_t convert(uint64_t x, const Field& f, uint2 k0, uint2 k1) {
+    return f.add(f.shoup(uint32_t(x), k0), f.shoup(uint32_t(x >> 32), k1));
+}
 
 // r[0..rlen) = a*b for a of la limbs, b of lb limbs, la + lb <= L (every
 // output limb, including the carry out of the top coefficient, falls inside
-// the L limbs the group produces); limbs beyond rlen are dropped.  `sm` is the group's MulSmem, `scr`
-// per-warp scratch of the block.  Every thread of the block must call this
-// with the same LG (the exchanges synchronise the block).
+// the L limbs the group produces); limbs beyond rlen are dropped.  `sm` is the
+// group's MulSmem, `scr` per-warp scratch of the block.  Every thread of the
+// block must call this with the same LG (the exchanges synchronise the block).
 template <int LG>
 __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_t la, const uint64_t* __restrict__ br,
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
-                                        uint64_t* sm, uint32_t* scr) {
+                                        uint32_t* sm, uint32_t* scr) {
     using Pl = Plan<LG>;
-    uint64_t* sh = sm;           // exchange buffer
-    uint64_t* res = sm + Pl::L;  // res[q][slot], q < 3
-    // a's spectrum waits in res[2]'s region: it is read back (by the thread
-    // that wrote it) before the inverse transform of the last prime, whose
-    // barriers order those reads before res[2] is written.
-    uint64_t* spec = res + 2 * Pl::L;
+    uint32_t* sh = sm;           // exchange buffer
+    uint32_t* res = sm + Pl::L;  // res[q][slot], q < 5
+    // a's spectrum waits in the last prime's residue array: it is read back
+    // (by the thread that wrote it) before the inverse transform of that
+    // prime, whose barriers order those reads before the array is written.
+    uint32_t* spec = res + (kPrimes - 1) * Pl::L;
     const uint32_t t = threadIdx.x % Pl::NT;
 #pragma unroll 1
-    for (int q = 0; q < 3; ++q) {
-        const FieldC32 f{P.p[q], 2 * P.p[q], P.c[q]};
-        const uint64_t ka = P.ka_by_lg[q][LG];
-        uint64_t x[8];
-        // a*(R/L)/R = a/L and b*R^2/R = b*R: the pointwise product is then
-        // a*b/L in plain form and the inverse needs no scaling.
+    for (int q = 0; q < kPrimes; ++q) {
+        const Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
+        const uint2 ka0 = P.ka_by_lg[q][LG - 8][0], ka1 = P.ka_by_lg[q][LG - 8][1];
+        uint32_t x[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
-            x[j] = (i < la) ? f.mul(__ldg(ar + i), ka) : 0;
+            x[j] = (i < la) ? convert(__ldg(ar + i), f, ka0, ka1) : 0u;
         }
         forward<LG>(x, sh, P.tw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; j += 2)
-            *reinterpret_cast<ulonglong2*>(spec + swz(8 * t + j)) = make_ulonglong2(x[j], x[j + 1]);
+        for (int j = 0; j < 8; j += 4)
+            *reinterpret_cast<uint4*>(spec + swz(8 * t + j)) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+        const uint2 kb0 = P.kb[q][0], kb1 = P.kb[q][1];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
-            x[j] = (i < lb) ? f.mul(__ldg(br + i), P.kb[q]) : 0;
+            x[j] = (i < lb) ? convert(__ldg(br + i), f, kb0, kb1) : 0u;
         }
         forward<LG>(x, sh, P.tw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-            const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(spec + swz(8 * t + j));
-            x[j] = f.mul(x[j], v.x);
-            x[j + 1] = f.mul(x[j + 1], v.y);
+        for (int j = 0; j < 8; j += 4) {
+            const uint4 v = *reinterpret_cast<const uint4*>(spec + swz(8 * t + j));
+            x[j] = f.mont(x[j], v.x);
+            x[j + 1] = f.mont(x[j + 1], v.y);
+            x[j + 2] = f.mont(x[j + 2], v.z);
+            x[j + 3] = f.mont(x[j + 3], v.w);
         }
         inverse<LG>(x, sh, P.itw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = reduce1(x[j], f.p);
+        for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = f.reduce(x[j]);
     }
     __syncthreads();
 
-    // Garner: x = r0 + q0*y1 + q0*q1*y2, three u64 words (< 2^139).
-    const FieldC32 f1{P.p[1], 2 * P.p[1], P.c[1]};
-    const FieldC32 f2{P.p[2], 2 * P.p[2], P.c[2]};
+    // Garner: y0 = r0, y_i = (...((r_i - y0) c_0i - y1) c_1i ... - y_(i-1)) c_(i-1)i
+    // mod p_i with c_ji = p_j^-1 mod p_i; x = y0 + p0 (y1 + p1 (y2 + p2 (y3 +
+    // p3 y4))) < 2^150, evaluated in 32-bit words.
     uint64_t s[11];
 #pragma unroll
     for (int w = 0; w < 11; ++w) s[w] = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j += 2) {
+    for (int j = 0; j < 8; j += 4) {
         const uint32_t slot = swz(8 * t + j);
-        const ulonglong2 r0 = *reinterpret_cast<const ulonglong2*>(res + slot);
-        const ulonglong2 r1 = *reinterpret_cast<const ulonglong2*>(res + Pl::L + slot);
-        const ulonglong2 r2 = *reinterpret_cast<const ulonglong2*>(res + 2 * Pl::L + slot);
+        uint4 rv[kPrimes];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint64_t v0 = h ? r0.y : r0.x, v1 = h ? r1.y : r1.x, v2 = h ? r2.y : r2.x;
-            const uint64_t y1 = reduce1(f1.mul(v1 + f1.p - v0, P.g01), f1.p);
-            const uint64_t u = reduce1(f2.mul(v2 + f2.p - v0, P.g02), f2.p);
-            const uint64_t y2 = reduce1(f2.mul(u + f2.p - y1, P.g12), f2.p);
-            const unsigned __int128 lo = (unsigned __int128)v0 + (unsigned __int128)P.p[0] * y1 +
-                                         (unsigned __int128)P.q01_lo * y2;  // < 2^127
-            const unsigned __int128 hi = (unsigned __int128)P.q01_hi * y2 + (uint64_t)(lo >> 64);
+        for (int q = 0; q < kPrimes; ++q) rv[q] = *reinterpret_cast<const uint4*>(res + q * Pl::L + slot);
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            uint32_t y[kPrimes];
+#pragma unroll
+            for (int q = 0; q < kPrimes; ++q)
+                y[q] = h == 0 ? rv[q].x : (h == 1 ? rv[q].y : (h == 2 ? rv[q].z : rv[q].w));
+            int c = 0;
+#pragma unroll
+            for (int i = 1; i < kPrimes; ++i) {
+                const Field fi{P.p[i], 2 * P.p[i], 0u};
+                uint32_t v = y[i];
+#pragma unroll
+                for (int k = 0; k < i; ++k) v = fi.shoup(v + fi.p2 - y[k], P.garner[c++]);
+                y[i] = fi.reduce(v);
+            }
+            // Horner in 32-bit words: acc = y4; acc = acc * p_i + y_i, i = 3..0
+            uint32_t acc[5] = {y[kPrimes - 1], 0u, 0u, 0u, 0u};
+#pragma unroll
+            for (int i = kPrimes - 2; i >= 0; --i) {
+                uint64_t carry = y[i];
+#pragma unroll
+                for (int w = 0; w < kPrimes - 1 - i; ++w) {
+                    const uint64_t tt = uint64_t(acc[w]) * P.p[i] + carry;
+                    acc[w] = uint32_t(tt);
+                    carry = tt >> 32;
+                }
+                acc[kPrimes - 1 - i] = uint32_t(carry);
+            }
+            const uint64_t w0 = uint64_t(acc[0]) | (uint64_t(acc[1]) << 32);
+            const uint64_t w1 = uint64_t(acc[2]) | (uint64_t(acc[3]) << 32);
+            const uint64_t w2 = acc[4];
             // add (w0, w1, w2) at word j+h of the thread's 8-limb block
             const int o = j + h;
-            unsigned __int128 acc = (unsigned __int128)s[o] + (uint64_t)lo;
-            s[o] = (uint64_t)acc;
-            acc = (unsigned __int128)s[o + 1] + (uint64_t)hi + (uint64_t)(acc >> 64);
-            s[o + 1] = (uint64_t)acc;
-            acc = (unsigned __int128)s[o + 2] + (uint64_t)(hi >> 64) + (uint64_t)(acc >> 64);
-            s[o + 2] = (uint64_t)acc;
+            unsigned __int128 a = (unsigned __int128)s[o] + w0;
+            s[o] = (uint64_t)a;
+            a = (unsigned __int128)s[o + 1] + w1 + (uint64_t)(a >> 64);
+            s[o + 1] = (uint64_t)a;
+            a = (unsigned __int128)s[o + 2] + w2 + (uint64_t)(a >> 64);
+            s[o + 2] = (uint64_t)a;
 #pragma unroll
             for (int w = o + 3; w < 11; ++w) {
-                acc = (unsigned __int128)s[w] + (uint64_t)(acc >> 64);
-                s[w] = (uint64_t)acc;
+                a = (unsigned __int128)s[w] + (uint64_t)(a >> 64);
+                s[w] = (uint64_t)a;
             }
         }
     }
     // words 8..10 overflow into the right neighbour's block
-    uint64_t* ov = sh;  // 3 words per thread
+    uint64_t* ov = reinterpret_cast<uint64_t*>(sh);  // 24 bytes x L/8 threads: fits the 4L bytes of sh
     ov[3 * t + 0] = s[8];
     ov[3 * t + 1] = s[9];
     ov[3 * t + 2] = s[10];
@@ -151,5 +183,5 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
     __syncthreads();  // sh and res are reused by the next call
 }
 
-}  // namespace ntt
+}  // namespace ntt32
 }  // namespace mi

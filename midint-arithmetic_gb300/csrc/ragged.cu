@@ -29,6 +29,7 @@
 #include "ctx.h"
 #include "kernels.h"
 #include "mul_core.cuh"
+#include "ntt32.cuh"
 #include "ntt_mul.cuh"
 
 namespace mi {
@@ -213,23 +214,23 @@ __device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
 // --- NTT family ----------------------------------------------------------------
 
 template <int LG>
-__device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint64_t* sm, uint32_t* scr_warp) {
+__device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32_t* sm, uint32_t* scr_warp) {
     constexpr int NT = (1 << LG) / 8;
     const uint32_t g = threadIdx.x / NT;
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
-    uint64_t* gsm = sm + g * ntt::MulSmem<LG>::WORDS64;
+    uint32_t* gsm = sm + g * ntt32::MulSmem<LG>::WORDS32;
     if (g < tk.count) {
         const mi_op op = P.ops[sorted[tk.first + g]];
-        ntt::mul_one<LG>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb, P.ntt, gsm,
-                         scr_warp);
+        ntt32::mul_one<LG>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb, P.ntt,
+                           gsm, scr_warp);
     } else {  // idle group: zero operands, no store, same barriers
-        ntt::mul_one<LG>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
+        ntt32::mul_one<LG>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
     }
 }
 
 __global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
-    extern __shared__ __align__(16) uint64_t smem[];
-    uint32_t* scr_warp = reinterpret_cast<uint32_t*>(smem + 8192);  // after 64 KiB
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the 48 KiB of groups
     __shared__ uint32_t s_task;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 0];
     for (;;) {
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
 
 // --- host side -------------------------------------------------------------------
 
-constexpr size_t kNttSmem = 65536 + 64;
+constexpr size_t kNttSmem = ntt32::MulSmem<11>::WORDS32 * 4 + 64;
 constexpr size_t kClsSmem = size_t(8) * CLS_WARP_WORDS * 4;
 
 std::mutex g_init_mu;
