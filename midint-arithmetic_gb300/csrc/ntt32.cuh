@@ -81,11 +81,18 @@ struct Plan {
 };
 
 // Moves the thread's 8 residues from layout (stride) d_from to d_to through
-// shared memory; the second barrier protects `sh` for the next exchange.
+// shared memory.  In a layout of stride d <= 32 the residues of a warp are the
+// 256 consecutive words of its own block, so an exchange between two such
+// layouts only synchronises the warp; the others synchronise the block.  The
+// first barrier makes every earlier read of the words about to be written
+// complete (the transforms start with a block-wide exchange, and between
+// transforms `sh` is only read by the thread that wrote it).
 template <int LG>
 __device__ __forceinline__ void exchange(uint32_t (&x)[8], uint32_t* sh, int d_from, int d_to) {
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
+    const bool local = P::NT <= 32 || (d_from <= 32 && d_to <= 32);
+    if (local) __syncwarp(); else __syncthreads();
     if (d_from == 1) {
 #pragma unroll
         for (int j = 0; j < 8; j += 4)
@@ -94,7 +101,7 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[8], uint32_t* sh, int d_f
 #pragma unroll
         for (int j = 0; j < 8; ++j) sh[swz(P::idx(d_from, t, j))] = x[j];
     }
-    __syncthreads();
+    if (local) __syncwarp(); else __syncthreads();
     if (d_to == 1) {
 #pragma unroll
         for (int j = 0; j < 8; j += 4) {
@@ -108,7 +115,6 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[8], uint32_t* sh, int d_f
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = sh[swz(P::idx(d_to, t, j))];
     }
-    __syncthreads();
 }
 
 // Forward transform (DIF).  In: x[j] = residue t + L/8*j (natural order),
