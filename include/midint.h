@@ -200,8 +200,8 @@ mi_status mi_export_words(mi_ctx ctx, const uint64_t* src, uint32_t n, uint32_t 
 
 /* ---------------------------------------------------------------------------
  * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 2048: every u64
- * limb is one digit, three 62-bit primes (the first is the reference's
- * FftPrime64, 29*2^57+1) carry the convolution, Garner's CRT and the final
+ * limb is one digit, five 30-bit primes carry the convolution (Shoup and
+ * Montgomery products on 32-bit residues), Garner's CRT and the final
  * carry run in the same kernel.  Replaces bmulFFT<P,M,Q>
  * (cuda/ker-fft-mul.cu.h:427-454) as launched by gpuMulFFT
  * (cuda/main.cu:415-520); unlike it, the result is exact at every size.

@@ -4,12 +4,15 @@
 // Fields (Montgomery form, R = 2^64, residues kept lazily in [0, 2p)):
 //  * FieldC32: p = c*2^32 + 1 < 2^62.  Since p = 1 mod 2^32, the per-word
 //    Montgomery factor is simply m = -t (no multiply), and m*p = m + (m*c)<<32,
-//    so one reduction is two 32x32 products plus carries.  The library's
-//    three primes are of this form; the first is the reference's FftPrime64
-//    (cuda/ker-fft-mul.cu.h:44-57: p = 29*2^57+1, g = 21, 2-adicity 57).
+//    so one reduction is two 32x32 products plus carries.  The reference's
+//    FftPrime64 (cuda/ker-fft-mul.cu.h:44-57: p = 29*2^57+1, g = 21,
+//    2-adicity 57) is of this form.
 //  * FieldGen: any odd p < 2^62, the textbook word-by-word Montgomery
-//    reduction with p' = -p^-1 mod 2^32.  Only used to run the same transform
-//    code on the reference's FftPrime32 known answers (p = 3*2^30+1).
+//    reduction with p' = -p^-1 mod 2^32, e.g. the reference's FftPrime32
+//    (p = 3*2^30+1).
+// This file serves the single-prime transform of mi_ntt_raw, which checks the
+// transform code on the reference's known answers with the reference's own
+// primes; the multiplication kernels use the 30-bit fields of ntt32.cuh.
 // Both replace zmod_t (cuda/ker-fft-mul.cu.h:76-140), whose multiply is a
 // `%` on the double-width product.
 //

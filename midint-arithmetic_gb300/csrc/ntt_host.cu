@@ -1,4 +1,4 @@
-// ntt_host.cu -- host setup of the NTT kernels: constants of the three primes,
+// ntt_host.cu -- host setup of the NTT kernels: constants of the five primes,
 // the resident twiddle tables of a context, and the raw single-prime
 // transform entry point used to check the transform against the reference's
 // known answers.
