@@ -498,7 +498,7 @@ def wide_section(args, ctx, dev, stream, world, rank) -> dict:
     sp = stream.cuda_stream
     hbm = measured_peaks().get("hbm_gbs")
     n, m = 16, 1 << 21
-    a, b = workloads.add_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 7, rank), worst_every=4)
+    a, b = workloads.add_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 7, rank), worst_every=8)
     with torch.cuda.stream(stream):
         da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(2)]
         db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(2)]
@@ -512,7 +512,7 @@ def wide_section(args, ctx, dev, stream, world, rank) -> dict:
     gbs = n * (3 * 8 * m + 1) / (ms * 1e-3) / 1e9
     del da, db, dr, dc
     torch.cuda.empty_cache()
-    return {"config": f"{n} pairs x {m} u64 limbs ({64 * m >> 20} Mbit), every 4th pair all-ones + 1 "
+    return {"config": f"{n} pairs x {m} u64 limbs ({64 * m >> 20} Mbit), every 8th pair all-ones + 1 "
                       "(carries through every tile); 2 rotating sets of 768 MiB",
             "ms_per_launch": ms, "GB/s": world * gbs, "frac_hbm": (gbs / hbm) if hbm else None,
             "device_status_ok": status == 0}

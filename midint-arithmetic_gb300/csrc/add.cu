@@ -205,14 +205,19 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
 // A tile is one 256-thread block over 64 bytes of each operand per thread
 // (2048 u64 limbs).  Tiles take their index from an atomic counter in launch
 // order, so every tile a tile waits for has already started and will finish
-// (no dependence on the scheduler).  Each tile adds its limbs with carry-in 0,
+// (no dependence on the scheduler).  A plain addition first reads the 32 limbs
+// below its tile: the nearest one whose sum is not all ones gives the
+// carry-in directly, which settles almost every tile of random data without
+// waiting (the tile then only publishes its inclusive status).  Otherwise, and
+// for 6a + 10b, each tile adds its limbs with carry-in 0,
 // publishes its status word -- inclusive (its true carry-out) when it does not
 // propagate a carry or is the first tile of its instance, otherwise an
-// aggregate that says "passes the carry-in through" -- then thread 0 walks back
+// aggregate that says "passes the carry-in through" -- then it walks back
 // over aggregates to the nearest inclusive status, bounded by spin_limit polls
 // of an unpublished word (then the error word is set and the tile carries on
 // with carry-in 0, so the kernel always completes), publishes its own
 // inclusive status, and the block redoes the carry pass with that carry-in.
+// The walk back is done by a warp, 32 predecessors per step.
 // Status word: bits 0-1 state (1 aggregate, 2 inclusive), bit 2 carry value.
 
 constexpr uint32_t ST_AGG = 1u, ST_INC = 2u;
@@ -249,6 +254,23 @@ __global__ void __launch_bounds__(256)
     L x[Q], y[Q], s[Q];
     load_chunk<L, Q, VEC>(a + off, start, m, true, x);
     load_chunk<L, Q, VEC>(b + off, start, m, true, y);
+    // Carry-in straight from the 32 limbs below the tile: the nearest limb
+    // whose sum is not all ones decides it (generate: 1, kill: 0).  Random
+    // limbs almost always settle it here and the tile never waits; only a
+    // run of 32 all-ones sums falls back to the look-back.
+    uint32_t local_cin = 0;
+    bool local_ok = j == 0;
+    if (OP == ADD_PLAIN && j > 0 && t < 32) {
+        const uint64_t i = uint64_t(j) * W - 1 - t;  // lane 0 is the limb just below the tile
+        const L ai = a[off + i], bi = b[off + i];
+        const L si = ai + bi;
+        const uint32_t settled = __ballot_sync(MI_FULL_MASK, si != L(~L(0)));
+        const uint32_t gen = __ballot_sync(MI_FULL_MASK, si < ai);
+        if (settled) {
+            local_ok = true;
+            local_cin = (gen >> (__ffs(settled) - 1)) & 1u;
+        }
+    }
     if constexpr (OP == ADD_SIX) {
         // 6a + 10b as lo + (hi shifted up one limb), as in k_add; thread 0
         // recomputes the high word of the limb before its tile
@@ -276,30 +298,42 @@ __global__ void __launch_bounds__(256)
     uint32_t gc0;
     (void)group_carry<256>(g, p, 0u, &gc0, scratch);
     const bool P = __syncthreads_and(p) != 0;  // the tile passes a carry-in through
-    if (t == 0) {
-        uint32_t cin = 0;
-        if (j > 0) {
-            st_release(status + tile, P ? ST_AGG : (ST_INC | (gc0 << 2)));
-            uint32_t k = tile - 1, spins = 0;
+    if (t < 32) {
+        // warp 0 looks back 32 tiles at a time: lane l reads tile k - l; the
+        // carry-in is the value of the nearest inclusive tile, valid once
+        // every tile between (all propagating aggregates) has published
+        uint32_t cin = local_cin;
+        if (!local_ok) {
+            if (t == 0) st_release(status + tile, P ? ST_AGG : (ST_INC | (gc0 << 2)));
+            const int32_t first = int32_t(tile - j);  // the instance's first tile: always inclusive
+            int32_t k = int32_t(tile) - 1;
+            uint32_t spins = 0;
             for (;;) {
-                const uint32_t sv = ld_acquire(status + k);
-                if ((sv & 3u) == ST_INC) {
-                    cin = (sv >> 2) & 1u;
-                    break;
-                }
-                if ((sv & 3u) == ST_AGG) {  // a propagating tile that is not its instance's first
-                    --k;
+                const int32_t i = k - int32_t(t);
+                const uint32_t sv = i >= first ? ld_acquire(status + i) : ST_INC;
+                const uint32_t inc = __ballot_sync(MI_FULL_MASK, (sv & 3u) == ST_INC);
+                const uint32_t pending = __ballot_sync(MI_FULL_MASK, (sv & 3u) == 0u);
+                const uint32_t nearest = inc ? uint32_t(__ffs(inc) - 1) : 32u;
+                const uint32_t nearer = nearest == 32u ? MI_FULL_MASK : ((1u << nearest) - 1u);
+                if (pending & nearer) {
+                    if (++spins > spin_limit) {
+                        if (t == 0) atomicOr(err, 1u);
+                        break;
+                    }
+                    __nanosleep(64);
                     continue;
                 }
-                if (++spins > spin_limit) {
-                    atomicOr(err, 1u);
+                if (inc) {
+                    cin = (__shfl_sync(MI_FULL_MASK, sv, int(nearest)) >> 2) & 1u;
                     break;
                 }
-                __nanosleep(64);
+                k -= 32;
             }
         }
-        if (!(withhold && j == 0)) st_release(status + tile, ST_INC | ((gc0 | (P ? cin : 0u)) << 2));
-        s_cin = cin;
+        if (t == 0) {
+            if (!(withhold && j == 0)) st_release(status + tile, ST_INC | ((gc0 | (P ? cin : 0u)) << 2));
+            s_cin = cin;
+        }
     }
     __syncthreads();
     uint32_t gc;
