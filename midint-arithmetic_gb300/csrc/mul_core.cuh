@@ -122,8 +122,8 @@ __device__ __forceinline__ void stage_a(uint32_t* gA, const uint32_t* __restrict
 }
 
 // Same for the B operand, in the two-plane layout: half h of block j is 16-byte
-// slot h*NT + j.
-template <int NT, bool VEC>
+// slot (h*NT + j)*G, G groups interleaving their planes.
+template <int NT, bool VEC, int G = 1>
 __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__ row, uint32_t n32, bool valid,
                                         uint32_t t) {
 #pragma unroll
@@ -139,10 +139,14 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
             if (w + 2 < n32) q.z = __ldcs(row + w + 2);
             if (w + 3 < n32) q.w = __ldcs(row + w + 3);
         }
-        gB4[(v & 1) * NT + (v >> 1)] = q;
+        gB4[((v & 1) * NT + (v >> 1)) * G] = q;
     }
 }
 
+// G > 1: G groups of a warp interleave their operands and slots so that the
+// warp's accesses of one step fall on distinct banks: A-block k of group g at
+// word (k*G + g)*T, B plane slot (h*NT + j)*G + g, pair w of lane l at
+// w*NT*G + g*NT + l (gA, gB4 and slots point at group g's first element).
 // The full product of the group's staged A (NT blocks) and B (NT blocks), of
 // which only the first nb hold nonzero limbs (1 <= nb <= NT).  Steps k >= nb
 // (A-block k zero for the whole group) are not run; anti-diagonal t is then
@@ -151,11 +155,11 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 // (pair w of thread l at slots[w*NT + l]), `scr` per-warp scratch for groups
 // wider than a warp.  Starts and ends with the group's shared areas free for
 // reuse by the caller after a group_sync.
-template <int NT>
+template <int NT, int G = 1>
 __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
                                                uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                                uint32_t nb = NT) {
-    auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NT + lane]; };
+    auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NT * G + lane]; };
     DiagAcc s;
 #pragma unroll
     for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
@@ -168,10 +172,10 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
     for (uint32_t k = 0; k < nb; ++k) {
         const uint32_t j = (t - k) & uint32_t(NT - 1);
         uint32_t A[T], B[T];
-        const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * T)[0];
-        const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * T)[1];
-        const uint4 b0 = gB4[j];
-        const uint4 b1 = gB4[NT + j];
+        const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * G * T)[0];
+        const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * G * T)[1];
+        const uint4 b0 = gB4[j * G];
+        const uint4 b1 = gB4[(NT + j) * G];
         A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
         A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
         B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;

@@ -269,15 +269,16 @@ __device__ __forceinline__ void load_chunk_regs(uint4 (&q)[classic::T / 4], cons
 template <int NT>
 __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* wsm) {
     using classic::T;
+    constexpr int G = 32 / NT;  // groups of the warp, interleaved in shared memory
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t g = lane / NT, t = lane % NT;
     if (g >= tk.count) return;  // groups synchronise only among their own lanes
     const uint32_t chunks = (tk.key - KEY_CLS) % 256 + 1;
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     const mi_op op = P.ops[sorted[tk.first + g]];
-    uint32_t* gA = wsm + g * NT * T;
-    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g * 2 * NT;
-    uint2* slots = reinterpret_cast<uint2*>(wsm + 512) + g * NT * classic::PAIRS;
+    uint32_t* gA = wsm + g * T;
+    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g;
+    uint2* slots = reinterpret_cast<uint2*>(wsm + 512) + g * NT;
     // longer operand x is consumed in chunks of W limbs against the staged shorter y
     const bool a_long = op.la >= op.lb;
     const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
@@ -286,7 +287,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     uint32_t* rr = reinterpret_cast<uint32_t*>(P.out + op.r_off);
     const uint32_t rlen = 2 * (op.la + op.lb);
     constexpr uint32_t W = NT * T;
-    classic::stage_b<NT, false>(gB4, y, ny, true, t);
+    classic::stage_b<NT, false, G>(gB4, y, ny, true, t);
     uint32_t pend[T];
 #pragma unroll
     for (int w = 0; w < T; ++w) pend[w] = 0;
@@ -295,11 +296,14 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     load_chunk_regs<NT>(nxt, x, nx, 0, t);
     for (uint32_t c = 0; c < chunks; ++c) {
 #pragma unroll
-        for (int it = 0; it < T / 4; ++it) reinterpret_cast<uint4*>(gA)[t + it * NT] = nxt[it];
+        for (int it = 0; it < T / 4; ++it) {  // 16-byte slot v: half v%2 of block v/2
+            const uint32_t v = t + it * NT;
+            reinterpret_cast<uint4*>(gA)[(v >> 1) * 2 * G + (v & 1)] = nxt[it];
+        }
         if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT>(gA, gB4, slots, nullptr, t, ulo, uhi);
+        classic::square_product<NT, G>(gA, gB4, slots, nullptr, t, ulo, uhi);
         // limbs [cW, (c+1)W) are final: the low half plus the pending window
         uint32_t fin[T];
         bool g0, p0;
@@ -431,11 +435,14 @@ mi_status init_device() {
     for (int k = 0; k < K_NTT; ++k) order[KEY_NTT + k] = uint16_t(KEY_NTT + (K_NTT - 1 - k));
     std::vector<int> cls(K_CLS);
     for (int k = 0; k < K_CLS; ++k) cls[k] = k;
-    // a chunk costs its NT tile steps plus a fixed overhead (operand load,
-    // carry passes, store) worth about kChunkOverhead steps
-    constexpr int kChunkOverhead = 8;
-    auto cost = [](int k) { return ((1 << (k / 256)) + kChunkOverhead) * (k % 256 + 1); };
-    std::stable_sort(cls.begin(), cls.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    // Group size first, ascending, then chunks, descending: consecutive tasks
+    // run the same code (one inlined square product per group size, so
+    // warps of an SM share their instructions), the long chunk chains of
+    // small groups -- latency-bound, one operand load per chunk -- start
+    // first, and the queue ends with the shortest tasks of the largest groups.
+    std::stable_sort(cls.begin(), cls.end(), [](int x, int y) {
+        return x / 256 != y / 256 ? x / 256 < y / 256 : x % 256 > y % 256;
+    });
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
     MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
