@@ -231,14 +231,14 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
 __global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the 48 KiB of groups
-    __shared__ uint32_t s_task;
+    __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 0];
-    for (;;) {
-        if (threadIdx.x == 0) s_task = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
-        __syncthreads();
-        const uint32_t t = s_task;
-        __syncthreads();
+    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
+    __syncthreads();
+    for (uint32_t it = 0;; ++it) {
+        const uint32_t t = s_task[it & 1];
         if (t >= ntasks) break;
+        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
         const Task tk = decode(P.scr, 0, t);
         switch (tk.key - KEY_NTT) {
             case 0: ntt_task<8>(P, tk, smem, scr_warp); break;
@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
             case 2: ntt_task<10>(P, tk, smem, scr_warp); break;
             default: ntt_task<11>(P, tk, smem, scr_warp); break;
         }
+        __syncthreads();  // the next index is visible; this one is read by all
     }
 }
 
@@ -392,14 +393,14 @@ __device__ __forceinline__ void add_task(const Params& P, const Task& tk, uint32
 
 __global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
     __shared__ uint32_t scr_warp[8];
-    __shared__ uint32_t s_task;
+    __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 2];
-    for (;;) {
-        if (threadIdx.x == 0) s_task = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
-        __syncthreads();
-        const uint32_t t = s_task;
-        __syncthreads();
+    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
+    __syncthreads();
+    for (uint32_t it = 0;; ++it) {
+        const uint32_t t = s_task[it & 1];
         if (t >= ntasks) break;
+        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
         const Task tk = decode(P.scr, 2, t);
         switch (tk.key - KEY_ADD) {
             case 0: add_task<2, 1>(P, tk, scr_warp); break;
@@ -413,6 +414,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
             case 8: add_task<4, 128>(P, tk, scr_warp); break;
             default: add_task<4, 256>(P, tk, scr_warp); break;
         }
+        __syncthreads();  // the next index is visible; this one is read by all
     }
 }
 
