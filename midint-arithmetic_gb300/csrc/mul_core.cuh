@@ -155,7 +155,10 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 // (pair w of thread l at slots[w*NT + l]), `scr` per-warp scratch for groups
 // wider than a warp.  Starts and ends with the group's shared areas free for
 // reuse by the caller after a group_sync.
-template <int NT, int G = 1>
+// Tile-loop unroll: deep for the plain kernels' wide groups (more loads in
+// flight per step), shallow where registers are short (small groups, the
+// ragged kernel's interleaved groups).
+template <int NT, int G = 1, int UNROLL = (NT >= 16 && G == 1) ? 8 : 2>
 __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
                                                uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                                uint32_t nb = NT) {
@@ -168,7 +171,7 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
 #pragma unroll
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
     const uint32_t snap_k = t < nb ? t : nb - 1;
-#pragma unroll 2
+#pragma unroll UNROLL
     for (uint32_t k = 0; k < nb; ++k) {
         const uint32_t j = (t - k) & uint32_t(NT - 1);
         uint32_t A[T], B[T];
@@ -315,7 +318,7 @@ __device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restri
 // zero block nb instead, which exists whenever they do.  On return thread t
 // holds output blocks t (ulo) and NH+t (uhi), fully carried; the carry out of
 // block NB-1 is dropped (the product mod 2^(32*T*NB)).
-template <int NH>
+template <int NH, int UNROLL = NH >= 16 ? 4 : 2>
 __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
                                             uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                             uint32_t nb = 2 * NH) {
@@ -330,7 +333,7 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
     const uint32_t H = (nb + 1) / 2;
     const bool mirror = t < H && t < nb - 1 - t;  // owns a second anti-diagonal
-#pragma unroll 2
+#pragma unroll UNROLL
     for (uint32_t k = 0; k <= nb; ++k) {
         const bool first = k <= t;
         uint32_t i = first ? k : k - t - 1;
