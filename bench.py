@@ -312,9 +312,12 @@ def run_ours(args):
     ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 0)
     copy_s = max_over_ranks(world, host_steps())
     ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, zero_copy)
-    path = ("mi_host_mul_full_u64 on pinned host buffers; the kernel reads the operands and writes the products "
-            "in place over the host link (zero-copy, the tuned choice for multiplications)" if zero_copy else
-            "mi_host_mul_full_u64 on pinned host buffers; chunked copy-in / compute / copy-out pipeline")
+    path = {0: "mi_host_mul_full_u64 on pinned host buffers; chunked copy-in / compute / copy-out pipeline",
+            1: "mi_host_mul_full_u64 on pinned host buffers; the kernel reads the operands and writes the products "
+               "in place over the host link (zero-copy, the tuned choice for multiplications)",
+            2: "mi_host_mul_full_u64 on pinned host buffers; the kernels read the operands in place over the host "
+               "link while the products of earlier chunks are copied out (the tuned choice for multiplications)"
+            }[zero_copy]
     e2e = {"value": world * N_MUL / e2e_s, "unit": "products/s", "h2d_bytes_per_step": 2 * in_bytes,
            "d2h_bytes_per_step": 2 * in_bytes, "ms_per_step": e2e_s * 1e3, "path": path,
            "copy_pipeline_ms_per_step": copy_s * 1e3}

@@ -97,10 +97,13 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
  *   MI_TUNE_HOST_CHUNKS      cls = 0 additions, 1 multiplications; value
  *                            1..64: chunks a host-buffer batch is cut into
  *                            for copy/compute overlap
- *   MI_TUNE_HOST_ZERO_COPY   cls as above; value 0 or 1: host-buffer calls
- *                            whose buffers are all mapped pinned memory run
- *                            the kernel on them in place (the buffers must
- *                            hold the whole batch, as for the copies) */
+ *   MI_TUNE_HOST_ZERO_COPY   cls as above; value 0: copies both ways;
+ *                            1: when every buffer is mapped pinned memory,
+ *                            the kernel reads and writes them in place;
+ *                            2: when the operands are mapped pinned memory,
+ *                            the kernel reads them in place and the results
+ *                            are copied out in chunks (the buffers must hold
+ *                            the whole batch, as for the copies) */
 enum {
     MI_TUNE_PLAIN_NTT_MIN = 0,
     MI_TUNE_RAGGED_NTT_MIN = 1,

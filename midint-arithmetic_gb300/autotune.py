@@ -183,19 +183,22 @@ def tune_host(ctx) -> tuple[list[int], list[int], dict]:
     record, chunks, zero_copy = {}, [], []
     for cls, name in ((0, "add"), (1, "mul")):
         cands = {}
-        for zc, ch in [(0, c) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1)]:
+        for zc, ch in [(0, c) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1)] + [(2, c) for c in (2, 3, 4, 6, 8, 12)]:
             ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
             ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
             cands[f"zero_copy={zc},chunks={ch}"] = {"zero_copy": zc, "chunks": ch, "ms": wall(calls[cls])}
-        # the chunk count serves callers whose buffers are not pinned even
-        # when zero-copy wins for pinned ones
-        best_copy = min((v for v in cands.values() if not v["zero_copy"]), key=lambda v: v["ms"])
-        zc = int(cands["zero_copy=1,chunks=1"]["ms"] < best_copy["ms"])
+        # the pipeline's chunk count also serves callers whose buffers are
+        # not pinned, so it is the best copy pipeline's unless mode 2 (which
+        # chunks the same way) wins
+        best_copy = min((v for v in cands.values() if v["zero_copy"] == 0), key=lambda v: v["ms"])
+        best = min(cands.values(), key=lambda v: v["ms"])
+        zc = best["zero_copy"]
+        ch = best["chunks"] if zc == 2 else best_copy["chunks"]
         ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
-        ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, best_copy["chunks"])
-        chunks.append(best_copy["chunks"])
+        ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
+        chunks.append(ch)
         zero_copy.append(zc)
-        record[name] = {"candidates": cands, "pick": {"chunks": best_copy["chunks"], "zero_copy": zc}}
+        record[name] = {"candidates": cands, "pick": {"chunks": ch, "zero_copy": zc}}
     return chunks, zero_copy, record
 
 
@@ -219,8 +222,9 @@ constexpr uint32_t kRaggedNttMin = {ragged};
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {{{add}}};
 // Host-buffer calls, by operation class {{additions, multiplications}}: chunks a
-// large batch is cut into for copy/compute overlap, and whether kernels read
-// mapped pinned host buffers in place (1) instead.
+// large batch is cut into for copy/compute overlap, and the zero-copy mode for
+// mapped pinned buffers (0 copies, 1 kernels read and write in place, 2 kernels
+// read the operands in place and the results are copied out).
 constexpr uint32_t kHostChunks[2] = {{{chunks}}};
 constexpr uint32_t kHostZeroCopy[2] = {{{zero_copy}}};
 

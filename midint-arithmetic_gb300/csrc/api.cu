@@ -179,8 +179,11 @@ mi_status wide_status(mi_ctx ctx) {
 }
 
 // Runs `launch(da, db, dr, dcarry, count, stream)` over a batch of host
-// buffers, with the tuning of operation class `cls`.  With zero-copy enabled
-// for the class and every buffer mapped pinned memory, one
+// buffers, with the tuning of operation class `cls`.  Zero-copy mode 2 with
+// mapped pinned operands: the kernels read the operands in place and only the
+// results go through the staging slots and the copy-out stream (the two
+// directions of the host link then run at once).  Zero-copy mode 1 with
+// every buffer mapped pinned memory: one
 // launch reads and writes them in place.  Otherwise the batch is cut into
 // chunks that cycle through kSlots device staging slots: chunk c copies in on
 // the copy-in stream (after the slot's previous copy-out), computes on compute
@@ -196,13 +199,20 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
     std::lock_guard<std::mutex> lk(ctx->mu);
+    // zero-copy reads of the operands (modes 1 and 2) when both are mapped
+    const char* za = nullptr;
+    const char* zb = nullptr;
     if (ctx->host_zero_copy[cls]) {
-        void* da = mapped_host(h_a);
-        void* db = mapped_host(h_b);
+        za = static_cast<const char*>(mapped_host(h_a));
+        zb = static_cast<const char*>(mapped_host(h_b));
+        if (!za || !zb) za = zb = nullptr;
+    }
+    if (za && ctx->host_zero_copy[cls] == 1) {
         void* dr = mapped_host(h_r);
         void* dc = h_carry ? mapped_host(h_carry) : nullptr;
-        if (da && db && dr && (dc || !h_carry)) {
-            MI_TRY(launch(da, db, dr, static_cast<uint8_t*>(dc), n, ctx->pipe[2]));
+        if (dr && (dc || !h_carry)) {
+            MI_TRY(launch(const_cast<char*>(za), const_cast<char*>(zb), dr, static_cast<uint8_t*>(dc), n,
+                          ctx->pipe[2]));
             MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[2]));
             return MI_OK;
         }
@@ -223,15 +233,23 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
         const int slot = c % mi_ctx_s::kSlots;
         cudaStream_t comp = ctx->pipe[one_compute_stream ? 2 : 2 + (c & 1)];
         char* stg = static_cast<char*>(ctx->stage[slot]);
-        if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
-        MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
-                                    cudaMemcpyHostToDevice, cin));
-        MI_CUDA_TRY(cudaMemcpyAsync(stg + off_b, static_cast<const char*>(h_b) + base * in_row, cnt * in_row,
-                                    cudaMemcpyHostToDevice, cin));
-        MI_CUDA_TRY(cudaEventRecord(ctx->ev_in[slot], cin));
-        MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_in[slot], 0));
-        MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt,
-                      comp));
+        if (za) {
+            // mode 2: the kernel reads this chunk's operands in place and
+            // writes the staging slot once its previous copy-out is done
+            if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_out[slot], 0));
+            MI_TRY(launch(const_cast<char*>(za) + base * in_row, const_cast<char*>(zb) + base * in_row, stg + off_r,
+                          h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt, comp));
+        } else {
+            if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
+            MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
+                                        cudaMemcpyHostToDevice, cin));
+            MI_CUDA_TRY(cudaMemcpyAsync(stg + off_b, static_cast<const char*>(h_b) + base * in_row, cnt * in_row,
+                                        cudaMemcpyHostToDevice, cin));
+            MI_CUDA_TRY(cudaEventRecord(ctx->ev_in[slot], cin));
+            MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_in[slot], 0));
+            MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr,
+                          cnt, comp));
+        }
         MI_CUDA_TRY(cudaEventRecord(ctx->ev_k[slot], comp));
         MI_CUDA_TRY(cudaStreamWaitEvent(cout, ctx->ev_k[slot], 0));
         MI_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_r) + base * out_row, stg + off_r, cnt * out_row,
@@ -374,7 +392,7 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             return MI_OK;
         case MI_TUNE_HOST_ZERO_COPY:
             if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
-            if (value > 1) return set_error(MI_EINVAL, "host zero-copy %u not 0 or 1", value);
+            if (value > 2) return set_error(MI_EINVAL, "host zero-copy mode %u not 0, 1 or 2", value);
             ctx->host_zero_copy[cls] = value;
             return MI_OK;
         case MI_TUNE_WIDE_SPIN_LIMIT:

@@ -18,8 +18,9 @@ constexpr uint32_t kRaggedNttMin = 129;
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32, 32, 64, 64};
 // Host-buffer calls, by operation class {additions, multiplications}: chunks a
-// large batch is cut into for copy/compute overlap, and whether kernels read
-// mapped pinned host buffers in place (1) instead.
+// large batch is cut into for copy/compute overlap, and the zero-copy mode for
+// mapped pinned buffers (0 copies, 1 kernels read and write in place, 2 kernels
+// read the operands in place and the results are copied out).
 constexpr uint32_t kHostChunks[2] = {4, 3};
 constexpr uint32_t kHostZeroCopy[2] = {0, 1};
 

@@ -81,11 +81,44 @@ def test_zero_copy_on_pinned_buffers(hctx):
     assert np.array_equal(r, ra) and np.array_equal(c, ca)
 
 
+@pytest.mark.parametrize("chunks", [1, 3, 8])
+@pytest.mark.parametrize("pinned_out", [False, True])
+def test_zero_copy_reads_with_copied_results(hctx, chunks, pinned_out):
+    """Mode 2: operands read in place, results copied out in chunks."""
+    for cls in (0, 1):
+        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, 2)
+        hctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, chunks)
+    n, m = 513, 64
+    a, b = carry_stress(n, m, seed=chunks + 7)
+    pa, pb = _pinned(a), _pinned(b)
+    if pinned_out:
+        pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+        hctx.host_mul_full(pa, pb, pr, n, m)
+        got = pr.numpy().view(np.uint64)
+    else:
+        got = np.zeros(2 * n * m, np.uint64)
+        hctx.host_mul_full(pa, pb, got, n, m)
+    assert np.array_equal(got, O.mul(a, b, m, True))
+    r = np.zeros(n * m, np.uint64)
+    c = np.zeros(n, np.uint8)
+    hctx.host_add(pa, pb, r, c, n, m)
+    ra, ca = O.add(a, b, m)
+    assert np.array_equal(r, ra) and np.array_equal(c, ca)
+    # a wide addition in this mode keeps its launches on one stream
+    mw = 5000
+    aw, bw = carry_stress(3, mw, seed=2)
+    rw = np.zeros(3 * mw, np.uint64)
+    cw = np.zeros(3, np.uint8)
+    hctx.host_add(_pinned(aw), _pinned(bw), rw, cw, 3, mw)
+    raw, caw = O.add(aw, bw, mw)
+    assert np.array_equal(rw, raw) and np.array_equal(cw, caw)
+
+
 def test_host_tuning_knobs_are_checked(hctx):
     with pytest.raises(midint.MidintError):
         hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 0, 0)
     with pytest.raises(midint.MidintError):
-        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 2)
+        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 3)
     with pytest.raises(midint.MidintError):
         hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 2, 4)
     hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 1, 5)
