@@ -122,7 +122,7 @@ __device__ __forceinline__ void stage_a(uint32_t* gA, const uint32_t* __restrict
 }
 
 // Same for the B operand, in the two-plane layout: half h of block j is 16-byte
-// slot (h*NT + j)*G, G groups interleaving their planes.
+// slot h*G*NT + j from the group's base (G groups side by side in each plane).
 template <int NT, bool VEC, int G = 1>
 __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__ row, uint32_t n32, bool valid,
                                         uint32_t t) {
@@ -139,13 +139,13 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
             if (w + 2 < n32) q.z = __ldcs(row + w + 2);
             if (w + 3 < n32) q.w = __ldcs(row + w + 3);
         }
-        gB4[((v & 1) * NT + (v >> 1)) * G] = q;
+        gB4[(v & 1) * G * NT + (v >> 1)] = q;
     }
 }
 
 // G > 1: G groups of a warp interleave their operands and slots so that the
 // warp's accesses of one step fall on distinct banks: A-block k of group g at
-// word (k*G + g)*T, B plane slot (h*NT + j)*G + g, pair w of lane l at
+// word (k*G + g)*T, B plane slot (h*G + g)*NT + j, pair w of lane l at
 // w*NT*G + g*NT + l (gA, gB4 and slots point at group g's first element).
 // The full product of the group's staged A (NT blocks) and B (NT blocks), of
 // which only the first nb hold nonzero limbs (1 <= nb <= NT).  Steps k >= nb
@@ -177,8 +177,8 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         uint32_t A[T], B[T];
         const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * G * T)[0];
         const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * G * T)[1];
-        const uint4 b0 = gB4[j * G];
-        const uint4 b1 = gB4[(NT + j) * G];
+        const uint4 b0 = gB4[j];
+        const uint4 b1 = gB4[G * NT + j];
         A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
         A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
         B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;

@@ -278,7 +278,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     const mi_op op = P.ops[sorted[tk.first + g]];
     uint32_t* gA = wsm + g * T;
-    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g;
+    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g * NT;
     uint2* slots = reinterpret_cast<uint2*>(wsm + 512) + g * NT;
     // longer operand x is consumed in chunks of W limbs against the staged shorter y
     const bool a_long = op.la >= op.lb;

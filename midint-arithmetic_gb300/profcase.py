@@ -10,6 +10,8 @@ when --warmup 1) with seeded inputs already resident on the device:
   poly    the same batch                        (k_poly)
   ntt     1024 x 1024 u64 limbs                 (k_ntt_mul)
   ragged  a mixed ragged list (--ragged-ops)    (k_classify, k_scan, k_scatter, k_rg_*)
+  wide    16 pairs x 2^21 u64 limbs             (k_add_wide)
+  convert the addition batch to big-endian 8-byte words and back (k_export, k_count_words, k_import)
 
 Usage: python midint-arithmetic_gb300/profcase.py [--ops add,mul,...] [--warmup 0|1]
 """
@@ -28,7 +30,7 @@ if HERE not in sys.path:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ops", default="add,add6,mul,mul_lo,poly,ntt,ragged")
+    ap.add_argument("--ops", default="add,add6,mul,mul_lo,poly,ntt,ragged,wide,convert")
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--ragged-ops", type=int, default=20000)
     args = ap.parse_args()
@@ -47,7 +49,7 @@ def main():
 
     calls = []
     ops = args.ops.split(",")
-    if "add" in ops or "add6" in ops:
+    if "add" in ops or "add6" in ops or "convert" in ops:
         a, b = workloads.add_pairs(n=65536, m=64)
         da, db = dput(a), dput(b)
         dr = torch.empty_like(da)
@@ -56,6 +58,10 @@ def main():
             calls.append(lambda: ctx.add(da, db, dr, 65536, 64, carry=dc, stream=sp))
         if "add6" in ops:
             calls.append(lambda: ctx.add6(da, db, dr, 65536, 64, stream=sp))
+        if "convert" in ops:
+            cw = torch.empty(65536, dtype=torch.int32, device=dev)
+            calls.append(lambda: ctx.export_words(da, 65536, 64, dr, 64, 8, 1, 1, counts=cw, stream=sp))
+            calls.append(lambda: ctx.import_words(dr, 65536, 64, 8, 1, 1, db, 64, stream=sp))
     if any(o in ops for o in ("mul", "mul_lo", "poly")):
         a, b = workloads.mul_pairs(n=16384, m=128)
         ma, mb = dput(a), dput(b)
@@ -71,6 +77,12 @@ def main():
         na, nb = dput(a), dput(b)
         nr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
         calls.append(lambda: ctx.mul_ntt(na, nb, nr, 1024, 1024, stream=sp))
+    if "wide" in ops:
+        wa, wb = workloads.add_pairs(n=16, m=1 << 21, worst_every=8)
+        xa, xb = dput(wa), dput(wb)
+        xr = torch.empty_like(xa)
+        xc = torch.empty(16, dtype=torch.uint8, device=dev)
+        calls.append(lambda: ctx.add(xa, xb, xr, 16, 1 << 21, carry=xc, stream=sp))
     if "ragged" in ops:
         rops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops)
         d_ops = torch.from_numpy(rops.view(np.uint8).copy()).to(dev)
