@@ -80,59 +80,75 @@ struct Plan {
     }
 };
 
-// Moves the thread's 8 residues from layout (stride) d_from to d_to through
-// shared memory.  In a layout of stride d <= 32 the residues of a warp are the
-// 256 consecutive words of its own block, so an exchange between two such
+// Moves the thread's 8 residues of each of NA arrays (each with its own L
+// words of `sh`) from layout (stride) d_from to d_to through shared memory.
+// In a layout of stride d <= 32 the residues of a warp are the 256
+// consecutive words of its own block, so an exchange between two such
 // layouts only synchronises the warp; the others synchronise the block.  The
 // first barrier makes every earlier read of the words about to be written
 // complete (the transforms start with a block-wide exchange, and between
 // transforms `sh` is only read by the thread that wrote it).
-template <int LG>
-__device__ __forceinline__ void exchange(uint32_t (&x)[8], uint32_t* sh, int d_from, int d_to) {
+template <int LG, int NA>
+__device__ __forceinline__ void exchange(uint32_t (&x)[NA][8], uint32_t* sh, int d_from, int d_to) {
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
     const bool local = P::NT <= 32 || (d_from <= 32 && d_to <= 32);
     if (local) __syncwarp(); else __syncthreads();
-    if (d_from == 1) {
 #pragma unroll
-        for (int j = 0; j < 8; j += 4)
-            *reinterpret_cast<uint4*>(sh + swz(P::idx(1, t, j))) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-    } else {
+    for (int q = 0; q < NA; ++q) {
+        uint32_t* s = sh + q * P::L;
+        if (d_from == 1) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) sh[swz(P::idx(d_from, t, j))] = x[j];
+            for (int j = 0; j < 8; j += 4)
+                *reinterpret_cast<uint4*>(s + swz(P::idx(1, t, j))) =
+                    make_uint4(x[q][j], x[q][j + 1], x[q][j + 2], x[q][j + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[swz(P::idx(d_from, t, j))] = x[q][j];
+        }
     }
     if (local) __syncwarp(); else __syncthreads();
-    if (d_to == 1) {
 #pragma unroll
-        for (int j = 0; j < 8; j += 4) {
-            const uint4 v = *reinterpret_cast<const uint4*>(sh + swz(P::idx(1, t, j)));
-            x[j] = v.x;
-            x[j + 1] = v.y;
-            x[j + 2] = v.z;
-            x[j + 3] = v.w;
+    for (int q = 0; q < NA; ++q) {
+        const uint32_t* s = sh + q * P::L;
+        if (d_to == 1) {
+#pragma unroll
+            for (int j = 0; j < 8; j += 4) {
+                const uint4 v = *reinterpret_cast<const uint4*>(s + swz(P::idx(1, t, j)));
+                x[q][j] = v.x;
+                x[q][j + 1] = v.y;
+                x[q][j + 2] = v.z;
+                x[q][j + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[q][j] = s[swz(P::idx(d_to, t, j))];
         }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = sh[swz(P::idx(d_to, t, j))];
     }
 }
 
-// Forward transform (DIF).  In: x[j] = residue t + L/8*j (natural order),
-// values in [0, 2p).  Out: layout stride 1 (x[j] = slot 8t+j of the
-// bit-reversed spectrum), values in [0, 2p).
-template <int LG>
-__device__ __forceinline__ void forward(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ tw, const Field& f) {
+// Forward transforms (DIF) of NA arrays in lockstep on one prime (each
+// twiddle is loaded once for all of them).  In: x[q][j] = residue t + L/8*j
+// (natural order), values in [0, 2p).  Out: layout stride 1 (x[q][j] = slot
+// 8t+j of the bit-reversed spectrum), values in [0, 2p).
+template <int LG, int NA>
+__device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, const uint2* __restrict__ tw,
+                                        const Field& f) {
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
     auto bf = [&](int j, int k, uint32_t e) {
-        const uint32_t u = x[j], v = x[k];
-        x[j] = f.add(u, v);
-        x[k] = f.shoup(u + f.p2 - v, __ldg(tw + e));
+        const uint2 w = __ldg(tw + e);
+#pragma unroll
+        for (int q = 0; q < NA; ++q) {
+            const uint32_t u = x[q][j], v = x[q][k];
+            x[q][j] = f.add(u, v);
+            x[q][k] = f.shoup(u + f.p2 - v, w);
+        }
     };
 #pragma unroll
     for (int k = 0; k < P::NF; ++k) {
         const int d = P::d(k);
-        if (k > 0) exchange<LG>(x, sh, P::d(k - 1), d);
+        if (k > 0) exchange<LG, NA>(x, sh, P::d(k - 1), d);
         const uint32_t off = t % d;
         const uint32_t mult = uint32_t(P::S) << (3 * k);  // (L / 8d) * S
 #pragma unroll
@@ -146,24 +162,28 @@ __device__ __forceinline__ void forward(uint32_t (&x)[8], uint32_t* sh, const ui
         for (int j = 0; j < 8; j += 2) bf(j, j + 1, off * 4 * mult);
     }
     if constexpr (P::R > 0) {
-        exchange<LG>(x, sh, P::d(P::NF - 1), 1);
+        exchange<LG, NA>(x, sh, P::d(P::NF - 1), 1);
         if constexpr (P::R == 2) {
             const uint2 w1 = __ldg(tw + uint32_t(P::L / 4) * P::S);
 #pragma unroll
-            for (int j = 0; j < 8; j += 4) {
-                const uint32_t u0 = x[j], v0 = x[j + 2], u1 = x[j + 1], v1 = x[j + 3];
-                x[j] = f.add(u0, v0);
-                x[j + 2] = f.sub(u0, v0);  // twiddle 1
-                x[j + 1] = f.add(u1, v1);
-                x[j + 3] = f.shoup(u1 + f.p2 - v1, w1);
-            }
+            for (int q = 0; q < NA; ++q)
+#pragma unroll
+                for (int j = 0; j < 8; j += 4) {
+                    const uint32_t u0 = x[q][j], v0 = x[q][j + 2], u1 = x[q][j + 1], v1 = x[q][j + 3];
+                    x[q][j] = f.add(u0, v0);
+                    x[q][j + 2] = f.sub(u0, v0);  // twiddle 1
+                    x[q][j + 1] = f.add(u1, v1);
+                    x[q][j + 3] = f.shoup(u1 + f.p2 - v1, w1);
+                }
         }
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {  // twiddle 1
-            const uint32_t u = x[j], v = x[j + 1];
-            x[j] = f.add(u, v);
-            x[j + 1] = f.sub(u, v);
-        }
+        for (int q = 0; q < NA; ++q)
+#pragma unroll
+            for (int j = 0; j < 8; j += 2) {  // twiddle 1
+                const uint32_t u = x[q][j], v = x[q][j + 1];
+                x[q][j] = f.add(u, v);
+                x[q][j + 1] = f.sub(u, v);
+            }
     }
 }
 
@@ -173,6 +193,7 @@ __device__ __forceinline__ void forward(uint32_t (&x)[8], uint32_t* sh, const ui
 template <int LG>
 __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ itw,
                                         const Field& f) {
+    uint32_t(&xs)[1][8] = reinterpret_cast<uint32_t(&)[1][8]>(x);
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
     auto bf = [&](int j, int k, uint32_t e) {
@@ -198,7 +219,7 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
                 x[j + 3] = f.sub(u1, v1);
             }
         }
-        exchange<LG>(x, sh, 1, P::d(P::NF - 1));
+        exchange<LG, 1>(xs, sh, 1, P::d(P::NF - 1));
     }
 #pragma unroll
     for (int k = P::NF - 1; k >= 0; --k) {
@@ -214,7 +235,7 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) bf(j, j + 4, (off + d * j) * mult);
-        if (k > 0) exchange<LG>(x, sh, d, P::d(k - 1));
+        if (k > 0) exchange<LG, 1>(xs, sh, d, P::d(k - 1));
     }
 }
 

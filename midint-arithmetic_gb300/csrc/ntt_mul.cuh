@@ -6,8 +6,9 @@
 // so five primes p_i < 2^30 (product 2^149.4) recover every coefficient
 // exactly by CRT.  For each prime the group converts a and b into the field
 // (a scaled by 1/L, so the inverse transform needs no scaling pass, and b by
-// 2^32, which the Montgomery pointwise product takes out again), runs two
-// forward transforms, multiplies pointwise and runs the inverse transform
+// 2^32, which the Montgomery pointwise product takes out again), runs the two
+// forward transforms in lockstep (shared twiddle loads and barriers),
+// multiplies pointwise in registers and runs the inverse transform
 // (ntt32.cuh), leaving the residues in shared memory.  It then recombines each
 // coefficient with Garner's mixed-radix formula (ten Shoup products by
 // constant inverses, then a Horner evaluation in 32-bit words), sums the
@@ -24,12 +25,12 @@
 namespace mi {
 namespace ntt32 {
 
-// Shared memory of one group, in 32-bit words: exchange buffer (L) + five
-// residue arrays (5L); a's spectrum waits in the last residue array.
+// Shared memory of one group, in 32-bit words: exchange buffers of a and b
+// (2L) + five residue arrays (5L).
 template <int LG>
 struct MulSmem {
     static constexpr int L = 1 << LG;
-    static constexpr size_t WORDS32 = size_t(6) * L;
+    static constexpr size_t WORDS32 = size_t(7) * L;
 };
 
 // x*K mod p in [0, 2p) for a 64-bit digit x: K0 = K mod p, K1 = 2^32 K mod p
@@ -48,45 +49,27 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
                                         uint32_t* sm, uint32_t* scr) {
     using Pl = Plan<LG>;
-    uint32_t* sh = sm;           // exchange buffer
-    uint32_t* res = sm + Pl::L;  // res[q][slot], q < 5
-    // a's spectrum waits in the last prime's residue array: it is read back
-    // (by the thread that wrote it) before the inverse transform of that
-    // prime, whose barriers order those reads before the array is written.
-    uint32_t* spec = res + (kPrimes - 1) * Pl::L;
+    uint32_t* sh = sm;               // exchange buffers of a and b (2L)
+    uint32_t* res = sm + 2 * Pl::L;  // res[q][slot], q < 5
     const uint32_t t = threadIdx.x % Pl::NT;
 #pragma unroll 1
     for (int q = 0; q < kPrimes; ++q) {
         const Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
         const uint2 ka0 = P.ka_by_lg[q][LG - 8][0], ka1 = P.ka_by_lg[q][LG - 8][1];
-        uint32_t x[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint32_t i = t + Pl::NT * j;
-            x[j] = (i < la) ? convert(__ldg(ar + i), f, ka0, ka1) : 0u;
-        }
-        forward<LG>(x, sh, P.tw[q], f);
-#pragma unroll
-        for (int j = 0; j < 8; j += 4)
-            *reinterpret_cast<uint4*>(spec + swz(8 * t + j)) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
         const uint2 kb0 = P.kb[q][0], kb1 = P.kb[q][1];
+        uint32_t x[2][8];  // a and b, transformed in lockstep
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
-            x[j] = (i < lb) ? convert(__ldg(br + i), f, kb0, kb1) : 0u;
+            x[0][j] = (i < la) ? convert(__ldg(ar + i), f, ka0, ka1) : 0u;
+            x[1][j] = (i < lb) ? convert(__ldg(br + i), f, kb0, kb1) : 0u;
         }
-        forward<LG>(x, sh, P.tw[q], f);
+        forward<LG, 2>(x, sh, P.tw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; j += 4) {
-            const uint4 v = *reinterpret_cast<const uint4*>(spec + swz(8 * t + j));
-            x[j] = f.mont(x[j], v.x);
-            x[j + 1] = f.mont(x[j + 1], v.y);
-            x[j + 2] = f.mont(x[j + 2], v.z);
-            x[j + 3] = f.mont(x[j + 3], v.w);
-        }
-        inverse<LG>(x, sh, P.itw[q], f);
+        for (int j = 0; j < 8; ++j) x[0][j] = f.mont(x[0][j], x[1][j]);
+        inverse<LG>(x[0], sh, P.itw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = f.reduce(x[j]);
+        for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = f.reduce(x[0][j]);
     }
     __syncthreads();
 
