@@ -81,7 +81,7 @@ mi_stream mi_ctx_stream(mi_ctx ctx);
 
 /* Classical/NTT crossovers of a context, in u64 limbs: ragged runs send a
  * product through the NTT kernel when its shorter operand has at least
- * ragged_ntt_min limbs (1..129; classical groups hold at most 128), and
+ * ragged_ntt_min limbs (1..257; classical groups hold at most 256), and
  * mi_mul_u64 does so when its operands have at least plain_ntt_min limbs
  * (1..1025; 1025 = never).  Defaults come from the committed tuning table. */
 mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min);
@@ -90,7 +90,7 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
  * that the project's autotuner measured and committed; these calls override
  * one entry (the autotuner itself sweeps candidates through them).
  *   MI_TUNE_PLAIN_NTT_MIN    cls ignored; value 1..1025 (as plain_ntt_min)
- *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..129 (as ragged_ntt_min)
+ *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..257 (as ragged_ntt_min)
  *   MI_TUNE_ADD_THREAD_BYTES cls = ceil(log2(u64 limbs)) 0..12 of the
  *                            operands; value = bytes of each operand one
  *                            thread owns: 16, 32 or 64

@@ -136,7 +136,7 @@ def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
     sp = stream.cuda_stream
     record = {}
     ref = None
-    for th in (16, 24, 32, 48, 64, 80, 96, 112, 128, 129):
+    for th in (32, 64, 96, 128, 160, 192, 224, 256, 257):
         ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, th)
         ms = _timer(lambda: ctx.ragged_run(d_ops, n_ops, d_in, d_out, scr, sb, carry=d_c, stream=sp), 5, 2, stream)
         out = d_out.cpu().numpy()
@@ -216,7 +216,7 @@ namespace tuned {{
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
 constexpr uint32_t kPlainNttMin = {plain};
 // Ragged runs: products whose shorter operand has at least this many u64
-// limbs use the NTT kernel (1..129).
+// limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = {ragged};
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.

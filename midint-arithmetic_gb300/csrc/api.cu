@@ -352,8 +352,8 @@ mi_stream mi_ctx_stream(mi_ctx ctx) { return ctx ? reinterpret_cast<mi_stream>(c
 
 mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min) {
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
-    if (ragged_ntt_min < 1 || ragged_ntt_min > 129)
-        return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..129", ragged_ntt_min);
+    if (ragged_ntt_min < 1 || ragged_ntt_min > 257)
+        return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..257", ragged_ntt_min);
     if (plain_ntt_min < 1 || plain_ntt_min > kNttMaxLimbs + 1)
         return set_error(MI_EINVAL, "plain_ntt_min %u outside 1..%u", plain_ntt_min, kNttMaxLimbs + 1);
     ctx->ragged_ntt_min = ragged_ntt_min;
@@ -376,7 +376,7 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             ctx->plain_ntt_min = value;
             return MI_OK;
         case MI_TUNE_RAGGED_NTT_MIN:
-            if (value < 1 || value > 129) return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..129", value);
+            if (value < 1 || value > 257) return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..257", value);
             ctx->ragged_ntt_min = value;
             return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:

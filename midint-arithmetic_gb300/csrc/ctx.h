@@ -26,8 +26,8 @@ struct mi_ctx_s {
     uint32_t host_zero_copy[2] = {mi::tuned::kHostZeroCopy[0], mi::tuned::kHostZeroCopy[1]};
     std::mutex mu;  // serialises host-pointer calls on one context
     // ragged batches: products whose shorter operand has at least this many
-    // u64 limbs go through the NTT kernel (at most 129: classical groups hold
-    // 128 limbs of the shorter operand)
+    // u64 limbs go through the NTT kernel (at most 257: classical groups hold
+    // 256 limbs of the shorter operand)
     uint32_t ragged_ntt_min = mi::tuned::kRaggedNttMin;
     // mi_mul_u64: square products of at least this many u64 limbs use the NTT
     uint32_t plain_ntt_min = mi::tuned::kPlainNttMin;

@@ -39,10 +39,13 @@ constexpr uint32_t kMaxLimbs = 1024;
 constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11
 constexpr int K_CLS = 6 * 256;   // NT = 1..32 x chunks = 1..256
 constexpr int K_ADD = 10;        // (Q=2, GS=1..32), (Q=4, GS=32..256)
-constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = K_NTT + K_CLS;
-constexpr int K = KEY_ADD + K_ADD;
+constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
+constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = K_NTT + K_CLS, KEY_C64 = KEY_ADD + K_ADD;
+constexpr int K = KEY_C64 + K_C64;
+constexpr int NFAM = 4;          // families: NTT, classical in a warp, additions, classical in 64 threads
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
+constexpr int C64_GROUP_WORDS = 512 + 512 + 64 * classic::PER_T;  // the same for one 64-thread group
 
 // Keys of each family in descending cost order (filled once per device).
 __constant__ uint16_t c_order[K];
@@ -51,10 +54,10 @@ struct Scratch {  // word offsets into the scratch buffer
     static constexpr size_t COUNTS = 0;
     static constexpr size_t CURSORS = COUNTS + K;
     static constexpr size_t OPOFF = CURSORS + K;
-    static constexpr size_t TS = OPOFF + K;             // task starts: K + 3 words (one extra per family)
-    static constexpr size_t NTASKS = TS + K + 3;        // 3 words
-    static constexpr size_t QUEUE = NTASKS + 3;         // 3 words
-    static constexpr size_t INVALID = QUEUE + 3;        // 1 word
+    static constexpr size_t TS = OPOFF + K;             // task starts: K + NFAM words (one extra per family)
+    static constexpr size_t NTASKS = TS + K + NFAM;     // NFAM words
+    static constexpr size_t QUEUE = NTASKS + NFAM;      // NFAM words
+    static constexpr size_t INVALID = QUEUE + NFAM;     // 1 word
     static constexpr size_t KEYS = ((INVALID + 1 + 31) / 32) * 32;
     __host__ __device__ static constexpr size_t sorted(uint32_t n) { return KEYS + n; }  // op indices by key
     __host__ __device__ static constexpr size_t words(uint32_t n) { return KEYS + 2 * size_t(n); }
@@ -89,6 +92,7 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
             const uint32_t lg = max(8u, ceil_log2(la + lb));
             return KEY_NTT + (lg - 8);
         }
+        if (s > 128) return KEY_C64 + (2 * l + 511) / 512 - 1;  // 64-thread groups, chunks of 256 limbs
         const uint32_t ntl = ceil_log2((2 * s + 7) / 8);  // NT = 2^ntl <= 32
         const uint32_t nt = 1u << ntl;
         const uint32_t chunks = (2 * l + 8 * nt - 1) / (8 * nt);
@@ -100,6 +104,7 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
     if (key < KEY_CLS) return 2048u >> (8 + key);                    // NTT: 256 threads / (L/8)
     if (key < KEY_ADD) return 32u >> ((key - KEY_CLS) / 256);        // classical: one warp
+    if (key >= KEY_C64) return 4u;                                    // classical: 256 threads / 64
     const uint32_t k = key - KEY_ADD;                                 // add: 256 threads / GS
     const uint32_t gs = k < 6 ? (1u << k) : (32u << (k - 6));
     return 256u / gs;
@@ -155,16 +160,16 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ scr) {
         __syncthreads();
     }
     // op offsets (exclusive, global over the ordered keys) and per-family task starts
-    const int fam_start[4] = {KEY_NTT, KEY_CLS, KEY_ADD, K};
+    const int fam_start[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, K};
     for (int i = threadIdx.x; i < K; i += blockDim.x) {
         const uint32_t key = c_order[i];
         scr[Scratch::OPOFF + key] = i ? s_ops[i - 1] : 0;
-        const int f = i < KEY_CLS ? 0 : (i < KEY_ADD ? 1 : 2);
+        const int f = i < KEY_CLS ? 0 : (i < KEY_ADD ? 1 : (i < KEY_C64 ? 2 : 3));
         const int base = fam_start[f];
         const uint32_t before = base ? s_tasks[base - 1] : 0;
         scr[Scratch::TS + f + i] = (i ? s_tasks[i - 1] : 0) - before;
     }
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < NFAM) {
         const int f = threadIdx.x;
         const int base = fam_start[f], end = fam_start[f + 1];
         const uint32_t before = base ? s_tasks[base - 1] : 0;
@@ -192,8 +197,8 @@ struct Task {
 };
 
 __device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
-    const int base = f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : KEY_ADD);
-    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS : K_ADD);
+    const int base = f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : KEY_C64));
+    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS : (f == 2 ? K_ADD : K_C64));
     const uint32_t* ts = scr + Scratch::TS + f + base;  // nk + 1 monotone starts
     int lo = 0, hi = nk;                                // ts[lo] <= t < ts[hi]
     while (hi - lo > 1) {
@@ -267,19 +272,29 @@ __device__ __forceinline__ void load_chunk_regs(uint4 (&q)[classic::T / 4], cons
     }
 }
 
+// One classical task: NT <= 32, 32/NT groups in the caller's warp (`sm` is the
+// warp's area, the groups interleaved); NT = 64, the four 64-thread groups of
+// the block (`sm` the block's area, one C64_GROUP_WORDS region per group;
+// groups without a product run on zeros so the block's barriers match, `scr`
+// holds the block's per-warp carry words).
 template <int NT>
-__device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* wsm) {
+__device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* sm, uint32_t* scr) {
     using classic::T;
-    constexpr int G = 32 / NT;  // groups of the warp, interleaved in shared memory
-    const uint32_t lane = threadIdx.x & 31u;
+    constexpr bool WIDE = NT > 32;
+    constexpr int G = WIDE ? 1 : 32 / NT;  // groups of the warp, interleaved in shared memory
+    const uint32_t lane = WIDE ? threadIdx.x : (threadIdx.x & 31u);
     const uint32_t g = lane / NT, t = lane % NT;
-    if (g >= tk.count) return;  // groups synchronise only among their own lanes
-    const uint32_t chunks = (tk.key - KEY_CLS) % 256 + 1;
+    const bool valid = g < tk.count;
+    if (!WIDE && !valid) return;  // warp groups synchronise only among their own lanes
+    const uint32_t chunks = WIDE ? tk.key - KEY_C64 + 1 : (tk.key - KEY_CLS) % 256 + 1;
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
-    const mi_op op = P.ops[sorted[tk.first + g]];
-    uint32_t* gA = wsm + g * T;
-    uint4* gB4 = reinterpret_cast<uint4*>(wsm + 256) + g * NT;
-    uint2* slots = reinterpret_cast<uint2*>(wsm + 512) + g * NT;
+    mi_op op{};
+    if (valid) op = P.ops[sorted[tk.first + g]];
+    uint32_t* gA = WIDE ? sm + g * C64_GROUP_WORDS : sm + g * T;
+    uint4* gB4 = WIDE ? reinterpret_cast<uint4*>(sm + g * C64_GROUP_WORDS + 512)
+                      : reinterpret_cast<uint4*>(sm + 256) + g * NT;
+    uint2* slots = WIDE ? reinterpret_cast<uint2*>(sm + g * C64_GROUP_WORDS + 1024)
+                        : reinterpret_cast<uint2*>(sm + 512) + g * NT;
     // longer operand x is consumed in chunks of W limbs against the staged shorter y
     const bool a_long = op.la >= op.lb;
     const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
@@ -304,15 +319,15 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT, G, 2>(gA, gB4, slots, nullptr, t, ulo, uhi);
+        classic::square_product<NT, G, 2>(gA, gB4, slots, scr, t, ulo, uhi);
         // limbs [cW, (c+1)W) are final: the low half plus the pending window
         uint32_t fin[T];
         bool g0, p0;
         uint32_t gc;
         chunk_add<uint32_t, T>(ulo, pend, fin, g0, p0);
-        const uint32_t cin = group_carry<NT>(g0, p0, 0u, &gc, nullptr);
+        const uint32_t cin = group_carry<NT>(g0, p0, 0u, &gc, scr);
         chunk_inc<uint32_t, T>(fin, cin);
-        classic::store_block<false>(rr, c * W + t * T, rlen, fin);
+        if (valid) classic::store_block<false>(rr, c * W + t * T, rlen, fin);
         // the high half plus that carry becomes the next window (cannot overflow)
         uint32_t z[T];
 #pragma unroll
@@ -321,11 +336,11 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         bool g1, p1;
         uint32_t gc1;
         chunk_add<uint32_t, T>(uhi, z, pend, g1, p1);
-        const uint32_t cin1 = group_carry<NT>(g1, p1, 0u, &gc1, nullptr);
+        const uint32_t cin1 = group_carry<NT>(g1, p1, 0u, &gc1, scr);
         chunk_inc<uint32_t, T>(pend, cin1);
         group_sync<NT>();  // gA and the slots are reused by the next chunk
     }
-    classic::store_block<false>(rr, chunks * W + t * T, rlen, pend);
+    if (valid) classic::store_block<false>(rr, chunks * W + t * T, rlen, pend);
 }
 
 __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
@@ -340,14 +355,32 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
         if (t >= ntasks) break;
         const Task tk = decode(P.scr, 1, t);
         switch ((tk.key - KEY_CLS) / 256) {
-            case 0: classic_task<1>(P, tk, wsm); break;
-            case 1: classic_task<2>(P, tk, wsm); break;
-            case 2: classic_task<4>(P, tk, wsm); break;
-            case 3: classic_task<8>(P, tk, wsm); break;
-            case 4: classic_task<16>(P, tk, wsm); break;
-            default: classic_task<32>(P, tk, wsm); break;
+            case 0: classic_task<1>(P, tk, wsm, nullptr); break;
+            case 1: classic_task<2>(P, tk, wsm, nullptr); break;
+            case 2: classic_task<4>(P, tk, wsm, nullptr); break;
+            case 3: classic_task<8>(P, tk, wsm, nullptr); break;
+            case 4: classic_task<16>(P, tk, wsm, nullptr); break;
+            default: classic_task<32>(P, tk, wsm, nullptr); break;
         }
         __syncwarp();
+    }
+}
+
+// Products whose shorter operand has 129..256 limbs (below the NTT crossover):
+// four 64-thread groups per block, one task = up to four products of one key.
+__global__ void __launch_bounds__(256, 2) k_rg_c64(Params P) {
+    extern __shared__ __align__(16) uint32_t smem32[];
+    __shared__ uint32_t scr_warp[8];
+    __shared__ uint32_t s_task[2];
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 3];
+    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 3, 1u);
+    __syncthreads();
+    for (uint32_t it = 0;; ++it) {
+        const uint32_t t = s_task[it & 1];
+        if (t >= ntasks) break;
+        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 3, 1u);
+        classic_task<64>(P, decode(P.scr, 3, t), smem32, scr_warp);
+        __syncthreads();  // the next index is visible; shared memory is reused
     }
 }
 
@@ -422,6 +455,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
 
 constexpr size_t kNttSmem = ntt32::MulSmem<11>::WORDS32 * 4 + 64;
 constexpr size_t kClsSmem = size_t(8) * CLS_WARP_WORDS * 4;
+constexpr size_t kC64Smem = size_t(4) * C64_GROUP_WORDS * 4;
 
 std::mutex g_init_mu;
 bool g_init[64] = {};
@@ -447,9 +481,11 @@ mi_status init_device() {
     });
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
+    for (int k = 0; k < K_C64; ++k) order[KEY_C64 + k] = uint16_t(KEY_C64 + (K_C64 - 1 - k));
     MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_classic, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kClsSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kC64Smem)));
     g_init[dev] = true;
     return MI_OK;
 }
@@ -478,8 +514,8 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     P.out = out;
     P.carry = carry;
     P.scr = static_cast<uint32_t*>(scratch);
-    // classical groups hold at most 32 tiles (128 u64 limbs) of the shorter operand
-    P.ntt_min = ntt_min < 1 ? 1 : (ntt_min > 129 ? 129 : ntt_min);
+    // classical groups hold at most 64 tiles (256 u64 limbs) of the shorter operand
+    P.ntt_min = ntt_min < 1 ? 1 : (ntt_min > 257 ? 257 : ntt_min);
     P.ntt = ctx->ntt.params;
     MI_CUDA_TRY(cudaMemsetAsync(P.scr, 0, (Scratch::KEYS) * 4, st));
     const uint32_t blocks = std::min<uint32_t>((n_ops + 255) / 256, uint32_t(sm_count() * 8));
@@ -488,6 +524,7 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     k_scatter<<<blocks, 256, 0, st>>>(n_ops, P.scr);
     k_rg_ntt<<<persistent_grid((const void*)k_rg_ntt, kNttSmem), 256, kNttSmem, st>>>(P);
     k_rg_classic<<<persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st>>>(P);
+    k_rg_c64<<<persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st>>>(P);
     k_rg_add<<<persistent_grid((const void*)k_rg_add, 0), 256, 0, st>>>(P);
     MI_CUDA_TRY(cudaGetLastError());
     return MI_OK;

@@ -171,7 +171,7 @@ def test_tuning_rejects_bad_values(ctx):
     with pytest.raises(midint.MidintError):
         ctx.set_tuning(midint.TUNE_ADD_THREAD_BYTES, 3, 24)
     with pytest.raises(midint.MidintError):
-        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, 130)
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, 258)
     with pytest.raises(midint.MidintError):
         ctx.set_tuning(99, 0, 1)
     old = ctx.get_tuning(midint.TUNE_PLAIN_NTT_MIN)

@@ -74,7 +74,7 @@ def edge_ops(seed, n_rand=600):
     la, lb, kind = [], [], []
     for k in (0, 1):
         for x in EDGE:
-            for y in (1, 4, 64, 128, 129, 1024, x):
+            for y in (1, 4, 64, 128, 129, 200, 256, 257, 1024, x):
                 la.append(x); lb.append(y); kind.append(k)
                 la.append(y); lb.append(x); kind.append(k)
     la += list(rng.integers(1, 1025, n_rand)); lb += list(rng.integers(1, 1025, n_rand))
@@ -82,7 +82,7 @@ def edge_ops(seed, n_rand=600):
     return W.pack_ops(np.array(kind, np.uint32), np.array(la, np.uint32), np.array(lb, np.uint32), seed)
 
 
-@pytest.mark.parametrize("ntt_min", [129, 64, 1])
+@pytest.mark.parametrize("ntt_min", [257, 200, 129, 64, 1])
 def test_ragged_matches_oracle(ctx, ntt_min):
     ops, pool, out_limbs = edge_ops(seed=ntt_min)
     # worst-case carries for some adds: a all ones, b = 1
@@ -93,26 +93,28 @@ def test_ragged_matches_oracle(ctx, ntt_min):
             pool[ao:ao + la] = np.uint64(2**64 - 1)
             pool[bo:bo + lb] = 0
             pool[bo] = 1
-    ctx.set_crossover(ntt_min, 256)
+    old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN)
+    ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, ntt_min)
     try:
         out, carry, invalid = run_ragged(ctx, ops, pool, out_limbs)
     finally:
-        ctx.set_crossover(129, 256)
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, old)
     assert invalid == 0
     oracle_check(ops, pool, out, carry)
 
 
 def test_ragged_all_ones_products(ctx):
     kind = np.ones(40, np.uint32)
-    la = np.array([1024, 1000, 129, 128, 64, 7, 1024, 300] * 5, np.uint32)
-    lb = np.array([1024, 3, 128, 129, 1024, 1024, 1, 300] * 5, np.uint32)
+    la = np.array([1024, 1000, 129, 128, 64, 7, 1024, 300, 256, 257] * 4, np.uint32)
+    lb = np.array([1024, 3, 128, 129, 1024, 1024, 1, 300, 1024, 200] * 4, np.uint32)
     ops, pool, out_limbs = W.pack_ops(kind, la, lb, 9)
     pool[:] = np.uint64(2**64 - 1)
-    for ntt_min in (129, 1):
-        ctx.set_crossover(ntt_min, 256)
+    old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN)
+    for ntt_min in (257, 200, 129, 1):
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, ntt_min)
         out, carry, _ = run_ragged(ctx, ops, pool, out_limbs)
         oracle_check(ops, pool, out, carry)
-    ctx.set_crossover(129, 256)
+    ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, old)
 
 
 def test_ragged_invalid_ops_are_skipped(ctx):
