@@ -40,7 +40,9 @@ constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11
 constexpr int K_CLS = 6 * 256;   // NT = 1..32 x chunks = 1..256
 constexpr int K_ADD = 10;        // (Q=2, GS=1..32), (Q=4, GS=32..256)
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
-constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = K_NTT + K_CLS, KEY_C64 = KEY_ADD + K_ADD;
+constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
+constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_CMB = KEY_CLS + K_CLS, KEY_ADD = KEY_CMB + K_CMB,
+              KEY_C64 = KEY_ADD + K_ADD;
 constexpr int K = KEY_C64 + K_C64;
 constexpr int NFAM = 4;          // families: NTT, classical in a warp, additions, classical in 64 threads
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
@@ -93,6 +95,11 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
             return KEY_NTT + (lg - 8);
         }
         if (s > 128) return KEY_C64 + (2 * l + 511) / 512 - 1;  // 64-thread groups, chunks of 256 limbs
+        if (s <= 8) {  // comb: 16 words of the longer operand per thread, 512 per pass of a warp
+            const uint32_t na = 2 * l;
+            if (na <= 256) return KEY_CMB + (na <= 64 ? 0 : (na <= 128 ? 1 : 2));
+            return KEY_CMB + 3 + (na + 511) / 512 - 1;
+        }
         const uint32_t ntl = ceil_log2((2 * s + 7) / 8);  // NT = 2^ntl <= 32
         const uint32_t nt = 1u << ntl;
         const uint32_t chunks = (2 * l + 8 * nt - 1) / (8 * nt);
@@ -103,7 +110,8 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
     if (key < KEY_CLS) return 2048u >> (8 + key);                    // NTT: 256 threads / (L/8)
-    if (key < KEY_ADD) return 32u >> ((key - KEY_CLS) / 256);        // classical: one warp
+    if (key < KEY_CMB) return 32u >> ((key - KEY_CLS) / 256);        // classical: one warp
+    if (key < KEY_ADD) return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;  // comb: 32 / group
     if (key >= KEY_C64) return 4u;                                    // classical: 256 threads / 64
     const uint32_t k = key - KEY_ADD;                                 // add: 256 threads / GS
     const uint32_t gs = k < 6 ? (1u << k) : (32u << (k - 6));
@@ -160,7 +168,7 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ scr) {
         __syncthreads();
     }
     // op offsets (exclusive, global over the ordered keys) and per-family task starts
-    const int fam_start[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, K};
+    const int fam_start[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, K};  // family 1 holds the comb keys too
     for (int i = threadIdx.x; i < K; i += blockDim.x) {
         const uint32_t key = c_order[i];
         scr[Scratch::OPOFF + key] = i ? s_ops[i - 1] : 0;
@@ -198,7 +206,7 @@ struct Task {
 
 __device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
     const int base = f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : KEY_C64));
-    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS : (f == 2 ? K_ADD : K_C64));
+    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS + K_CMB : (f == 2 ? K_ADD : K_C64));
     const uint32_t* ts = scr + Scratch::TS + f + base;  // nk + 1 monotone starts
     int lo = 0, hi = nk;                                // ts[lo] <= t < ts[hi]
     while (hi - lo > 1) {
@@ -343,6 +351,97 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     if (valid) classic::store_block<false>(rr, chunks * W + t * T, rlen, pend);
 }
 
+// Comb products, shorter operand y of at most 8 limbs (16 words, held in
+// registers by every thread of the group): thread t multiplies its 16 words
+// of the longer operand x by y (row carry chains in 64-bit arithmetic), keeps
+// the low 16 words and hands the high 16 to thread t+1, whose low words they
+// overlap; one carry-lookahead pass over the group makes 16 result words per
+// thread final, and the last thread's high words plus the carry-out open the
+// next pass (512 words of x per pass of a warp) -- a few passes where the
+// chunked square products would chain one chunk per 8 or 16 words.
+template <int G>
+__device__ __forceinline__ void comb_task(const Params& P, const Task& tk) {
+    constexpr int K = 16, NBW = 16;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t g = lane / G, t = lane % G;
+    if (g >= tk.count) return;  // groups synchronise only among their own lanes
+    const uint32_t ki = tk.key - KEY_CMB;
+    const uint32_t passes = ki < 3 ? 1u : ki - 2;
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    const mi_op op = P.ops[sorted[tk.first + g]];
+    const bool a_long = op.la >= op.lb;
+    const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
+    const uint32_t* y = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.b_off : op.a_off));
+    const uint32_t nx = 2 * (a_long ? op.la : op.lb), ny = 2 * (a_long ? op.lb : op.la);
+    uint32_t* rr = reinterpret_cast<uint32_t*>(P.out + op.r_off);
+    const uint32_t rlen = 2 * (op.la + op.lb);
+    const uint32_t mask = group_lanes<G>();
+    uint32_t B[NBW];
+#pragma unroll
+    for (int j = 0; j < NBW; j += 2) {  // limbs are 8-byte aligned pairs of words
+        const uint2 v = uint32_t(j + 2) <= ny ? __ldg(reinterpret_cast<const uint2*>(y + j)) : make_uint2(0, 0);
+        B[j] = v.x;
+        B[j + 1] = v.y;
+    }
+    uint32_t pend[NBW];
+#pragma unroll
+    for (int j = 0; j < NBW; ++j) pend[j] = 0;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const uint32_t base = (p * G + t) * K;
+        uint32_t a[K];
+#pragma unroll
+        for (int i = 0; i < K; i += 2) {
+            const uint2 v = base + i + 2 <= nx ? __ldcs(reinterpret_cast<const uint2*>(x + base + i)) : make_uint2(0, 0);
+            a[i] = v.x;
+            a[i + 1] = v.y;
+        }
+        uint32_t acc[K + NBW];
+#pragma unroll
+        for (int w = 0; w < NBW; ++w) acc[w] = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            uint64_t c = 0;
+#pragma unroll
+            for (int j = 0; j < NBW; ++j) {
+                const uint64_t v = uint64_t(a[i]) * B[j] + acc[i + j] + c;  // < 2^64
+                acc[i + j] = uint32_t(v);
+                c = v >> 32;
+            }
+            acc[i + NBW] = uint32_t(c);
+        }
+        // words [base, base + K): the low words plus the previous thread's
+        // high words (the pending words for the group's first thread)
+        uint32_t lo[K], hin[K], out[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t v = __shfl_up_sync(mask, acc[K + j], 1, G);
+            hin[j] = t == 0 ? pend[j] : v;
+            lo[j] = acc[j];
+        }
+        bool gg, pp;
+        uint32_t gc;
+        chunk_add<uint32_t, K>(lo, hin, out, gg, pp);
+        chunk_inc<uint32_t, K>(out, group_carry<G>(gg, pp, 0u, &gc, nullptr));
+#pragma unroll
+        for (int w = 0; w < K; ++w)
+            if (base + w < rlen) rr[base + w] = out[w];
+        // the last thread's high words plus the group's carry-out open the next pass
+        uint32_t c = gc;
+#pragma unroll
+        for (int j = 0; j < NBW; ++j) {
+            const uint64_t v = uint64_t(__shfl_sync(mask, acc[K + j], G - 1, G)) + c;
+            pend[j] = uint32_t(v);
+            c = uint32_t(v >> 32);
+        }
+    }
+    if (t == 0) {
+        const uint32_t top = passes * G * K;
+#pragma unroll
+        for (int w = 0; w < NBW; ++w)
+            if (top + w < rlen) rr[top + w] = pend[w];
+    }
+}
+
 __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
     extern __shared__ __align__(16) uint32_t smem32[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -354,6 +453,15 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
         t = __shfl_sync(MI_FULL_MASK, t, 0);
         if (t >= ntasks) break;
         const Task tk = decode(P.scr, 1, t);
+        if (tk.key >= uint32_t(KEY_CMB)) {
+            const uint32_t ki = tk.key - KEY_CMB;
+            if (ki == 0) comb_task<4>(P, tk);
+            else if (ki == 1) comb_task<8>(P, tk);
+            else if (ki == 2) comb_task<16>(P, tk);
+            else comb_task<32>(P, tk);
+            __syncwarp();
+            continue;
+        }
         switch ((tk.key - KEY_CLS) / 256) {
             case 0: classic_task<1>(P, tk, wsm, nullptr); break;
             case 1: classic_task<2>(P, tk, wsm, nullptr); break;
@@ -480,6 +588,9 @@ mi_status init_device() {
         return x / 256 != y / 256 ? x / 256 < y / 256 : x % 256 > y % 256;
     });
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
+    // comb keys after them, the most passes first
+    const int comb[K_CMB] = {6, 5, 4, 3, 2, 1, 0};
+    for (int k = 0; k < K_CMB; ++k) order[KEY_CMB + k] = uint16_t(KEY_CMB + comb[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
     for (int k = 0; k < K_C64; ++k) order[KEY_C64 + k] = uint16_t(KEY_C64 + (K_C64 - 1 - k));
     MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
