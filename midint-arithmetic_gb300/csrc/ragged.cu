@@ -100,9 +100,13 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
             if (na <= 256) return KEY_CMB + (na <= 64 ? 0 : (na <= 128 ? 1 : 2));
             return KEY_CMB + 3 + (na + 511) / 512 - 1;
         }
-        const uint32_t ntl = ceil_log2((2 * s + 7) / 8);  // NT = 2^ntl <= 32
+        // NT threads, NT-block chunks of the longer operand against the
+        // shorter one (whose blocks set the steps per chunk): as wide as the
+        // longer operand up to one warp, and never narrower than the shorter
+        const uint32_t nbs = (2 * s + 7) / 8, nbl = (2 * l + 7) / 8;
+        const uint32_t ntl = ceil_log2(max(nbs, min(nbl, 32u)));  // NT = 2^ntl <= 32
         const uint32_t nt = 1u << ntl;
-        const uint32_t chunks = (2 * l + 8 * nt - 1) / (8 * nt);
+        const uint32_t chunks = (nbl + nt - 1) / nt;
         return KEY_CLS + ntl * 256 + (chunks - 1);
     }
     return KEY_INVALID;
@@ -311,23 +315,31 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     uint32_t* rr = reinterpret_cast<uint32_t*>(P.out + op.r_off);
     const uint32_t rlen = 2 * (op.la + op.lb);
     constexpr uint32_t W = NT * T;
-    classic::stage_b<NT, false, G>(gB4, y, ny, true, t);
+    // the shorter operand y is the broadcast side (its nby blocks set the
+    // steps of every chunk), chunks of x are the two-plane side
+    const uint32_t nby = (ny + T - 1) / T;
+    uint4 nxt[T / 4];
+    load_chunk_regs<NT>(nxt, y, ny, 0, t);
+#pragma unroll
+    for (int it = 0; it < T / 4; ++it) {  // 16-byte slot v: half v%2 of block v/2
+        const uint32_t v = t + it * NT;
+        reinterpret_cast<uint4*>(gA)[(v >> 1) * 2 * G + (v & 1)] = nxt[it];
+    }
     uint32_t pend[T];
 #pragma unroll
     for (int w = 0; w < T; ++w) pend[w] = 0;
     // chunk c+1 of x is loaded into registers while chunk c is multiplied
-    uint4 nxt[T / 4];
     load_chunk_regs<NT>(nxt, x, nx, 0, t);
     for (uint32_t c = 0; c < chunks; ++c) {
 #pragma unroll
-        for (int it = 0; it < T / 4; ++it) {  // 16-byte slot v: half v%2 of block v/2
+        for (int it = 0; it < T / 4; ++it) {  // half v%2 of block v/2, plane layout
             const uint32_t v = t + it * NT;
-            reinterpret_cast<uint4*>(gA)[(v >> 1) * 2 * G + (v & 1)] = nxt[it];
+            gB4[(v & 1) * G * NT + (v >> 1)] = nxt[it];
         }
         if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT, G, 2>(gA, gB4, slots, scr, t, ulo, uhi);
+        classic::square_product<NT, G, 2>(gA, gB4, slots, scr, t, ulo, uhi, valid ? (nby ? nby : 1u) : 1u);
         // limbs [cW, (c+1)W) are final: the low half plus the pending window
         uint32_t fin[T];
         bool g0, p0;
