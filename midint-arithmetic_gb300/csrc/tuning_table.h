@@ -10,7 +10,7 @@ namespace mi {
 namespace tuned {
 
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
-constexpr uint32_t kPlainNttMin = 320;
+constexpr uint32_t kPlainNttMin = 256;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = 128;

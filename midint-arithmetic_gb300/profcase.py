@@ -12,12 +12,16 @@ when --warmup 1) with seeded inputs already resident on the device:
   ragged  a mixed ragged list (--ragged-ops)    (k_classify, k_scan, k_scatter, k_rg_*)
   wide    16 pairs x 2^21 u64 limbs             (k_add_wide)
   convert the addition batch to big-endian 8-byte words and back (k_export, k_count_words, k_import)
+  ragged_bands  the --ragged-ops list cut into its additions and its products
+          by shorter-operand band, each band timed alone as its own captured
+          ragged run (CUDA events over 10 replays after 3) and printed as JSON
 
 Usage: python midint-arithmetic_gb300/profcase.py [--ops add,mul,...] [--warmup 0|1]
 """
 from __future__ import annotations
 
 import argparse
+import json
 import os
 import sys
 
@@ -100,8 +104,53 @@ def main():
     for c in calls:
         c()
     torch.cuda.synchronize()
+    if "ragged_bands" in ops:
+        print(json.dumps(ragged_bands(ctx, dev, sp, args.ragged_ops), indent=1))
     ctx.close()
     print("profcase: ran", ",".join(ops))
+
+
+# (name, kind, lowest shorter-operand limbs, highest) of each band
+BANDS = (("adds", 0, 1, 1024), ("mul 1..8", 1, 1, 8), ("mul 9..16", 1, 9, 16), ("mul 17..32", 1, 17, 32),
+         ("mul 33..64", 1, 33, 64), ("mul 65..127", 1, 65, 127), ("mul >=128", 1, 128, 1024))
+
+
+def ragged_bands(ctx, dev, sp, n_ops: int) -> dict:
+    """Each band of the ragged list run alone: ops, ms per run and the
+    32x32-bit partial products of the classical product per second."""
+    import torch
+
+    import midint
+    import workloads
+
+    rops, _, _ = workloads.ragged_ops(n_ops=n_ops)
+    kind, la, lb = rops["kind"], rops["la"], rops["lb"]
+    short = np.minimum(la, lb)
+    res = {}
+    for name, k, lo, hi in (("all", -1, 1, 1024),) + BANDS:
+        sel = (short >= lo) & (short <= hi) & ((kind == k) if k >= 0 else True)
+        o, pool, out_limbs = workloads.pack_ops(kind[sel].astype(np.uint32), la[sel].astype(np.uint32),
+                                                lb[sel].astype(np.uint32), workloads.SEED_BASE + 5)
+        d_ops = torch.from_numpy(o.view(np.uint8).copy()).to(dev)
+        d_in = torch.from_numpy(pool.view(np.int64)).to(dev)
+        d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+        d_c = torch.empty(o.size, dtype=torch.uint8, device=dev)
+        sb = midint.ragged_scratch_bytes(o.size)
+        scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+        g = ctx.ragged_graph(d_ops, o.size, d_in, d_out, scr, sb, carry=d_c)
+        for _ in range(3):
+            g.launch(sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            g.launch(sp)
+        e1.record()
+        e1.synchronize()
+        g.close()
+        ms = e0.elapsed_time(e1) / 10
+        pp = int((4 * la[sel].astype(np.int64) * lb[sel].astype(np.int64) * (kind[sel] == 1)).sum())
+        res[name] = {"ops": int(sel.sum()), "ms": ms, "G_pp_per_s": pp / ms / 1e6}
+    return res
 
 
 if __name__ == "__main__":
