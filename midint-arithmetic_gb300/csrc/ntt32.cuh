@@ -24,9 +24,11 @@
 // element, and reads each twiddle from global memory (fft/ifft,
 // cuda/ker-fft-mul.cu.h:304-368).
 //
-// Twiddles: tw[e] = (w^e, floor(w^e 2^32 / p)) and itw[e] the same for w^-e,
-// e < 2048, w a primitive 4096th root of unity; a length-L transform reads
-// every (4096/L)-th entry.
+// Twiddles: pairs (w^e, floor(w^e 2^32 / p)) for the forward table and the
+// same for w^-e for the inverse, w a primitive 4096th root of unity, stored in
+// the order the passes read them (TwLayout): the lanes of a warp read
+// consecutive entries, a few cache lines per load instead of one line per
+// lane as in a table indexed by exponent.
 #pragma once
 
 #include <cstdint>
@@ -34,9 +36,35 @@
 namespace mi {
 namespace ntt32 {
 
-constexpr int kLgMax = 12;                     // 4096-point transforms at most
-constexpr int kTwiddles = (1 << kLgMax) / 2;   // entries per table
+constexpr int kLgMin = 8, kLgMax = 12;         // 256- to 4096-point transforms
+constexpr int kTwiddles = (1 << kLgMax) / 2;   // powers w^e, e < 2048, that the passes use
 constexpr int kPrimes = 5;
+
+// Twiddle table layout of one prime and direction.  For a length-2^LG
+// transform, radix-8 pass k has stride d = L / 8^(k+1) and twiddle step
+// m = 4096 / (8d); its butterflies at offset o = t mod d use w^((o + dj) m)
+// (stage 1, j < 4), w^(2 (o + dh) m) (stage 2, h < 2) and w^(4 o m) (stage 3).
+// The pass's entries are stage 1's 4d powers by o + dj, then stage 2's 2d by
+// o + dh, then stage 3's d by o; after the last pass one entry w^1024 (the
+// radix-4 step of the final pass).  Sections are rounded up to 16 entries.
+struct TwLayout {
+    __host__ __device__ static constexpr int nf(int lg) { return lg / 3; }
+    __host__ __device__ static constexpr int d(int lg, int k) { return (1 << lg) >> (3 * (k + 1)); }
+    // start of pass k inside the section of lg
+    __host__ __device__ static constexpr int pass(int lg, int k) {
+        int s = 0;
+        for (int i = 0; i < k; ++i) s += 7 * d(lg, i);
+        return s;
+    }
+    __host__ __device__ static constexpr int quarter(int lg) { return pass(lg, nf(lg)); }
+    __host__ __device__ static constexpr int size(int lg) { return (quarter(lg) + 1 + 15) / 16 * 16; }
+    __host__ __device__ static constexpr int base(int lg) {
+        int s = 0;
+        for (int g = kLgMin; g < lg; ++g) s += size(g);
+        return s;
+    }
+};
+constexpr int kTwEntries = TwLayout::base(kLgMax + 1);  // per prime and direction
 
 struct Field {
     uint32_t p, p2, pinv;  // pinv = -p^-1 mod 2^32
@@ -132,10 +160,11 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NA][8], uint32_t* sh, int
 // (natural order), values in [0, 2p).  Out: layout stride 1 (x[q][j] = slot
 // 8t+j of the bit-reversed spectrum), values in [0, 2p).
 template <int LG, int NA>
-__device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, const uint2* __restrict__ tw,
+__device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, const uint2* __restrict__ tw_all,
                                         const Field& f) {
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
+    const uint2* __restrict__ tw = tw_all + TwLayout::base(LG);
     auto bf = [&](int j, int k, uint32_t e) {
         const uint2 w = __ldg(tw + e);
 #pragma unroll
@@ -149,22 +178,21 @@ __device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, cons
     for (int k = 0; k < P::NF; ++k) {
         const int d = P::d(k);
         if (k > 0) exchange<LG, NA>(x, sh, P::d(k - 1), d);
-        const uint32_t off = t % d;
-        const uint32_t mult = uint32_t(P::S) << (3 * k);  // (L / 8d) * S
+        const uint32_t off = t % d, e0 = TwLayout::pass(LG, k) + off;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf(j, j + 4, (off + d * j) * mult);
+        for (int j = 0; j < 4; ++j) bf(j, j + 4, e0 + d * j);
 #pragma unroll
         for (int j = 0; j < 8; j += 4) {
-            bf(j, j + 2, off * 2 * mult);
-            bf(j + 1, j + 3, (off + d) * 2 * mult);
+            bf(j, j + 2, e0 + 4 * d);
+            bf(j + 1, j + 3, e0 + 5 * d);
         }
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) bf(j, j + 1, off * 4 * mult);
+        for (int j = 0; j < 8; j += 2) bf(j, j + 1, e0 + 6 * d);
     }
     if constexpr (P::R > 0) {
         exchange<LG, NA>(x, sh, P::d(P::NF - 1), 1);
         if constexpr (P::R == 2) {
-            const uint2 w1 = __ldg(tw + uint32_t(P::L / 4) * P::S);
+            const uint2 w1 = __ldg(tw + TwLayout::quarter(LG));
 #pragma unroll
             for (int q = 0; q < NA; ++q)
 #pragma unroll
@@ -191,11 +219,12 @@ __device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, cons
 // bit-reversed spectrum; out: x[j] = residue t + L/8*j in natural order;
 // values in [0, 2p) throughout.
 template <int LG>
-__device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ itw,
+__device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ itw_all,
                                         const Field& f) {
     uint32_t(&xs)[1][8] = reinterpret_cast<uint32_t(&)[1][8]>(x);
     using P = Plan<LG>;
     const uint32_t t = threadIdx.x % P::NT;
+    const uint2* __restrict__ itw = itw_all + TwLayout::base(LG);
     auto bf = [&](int j, int k, uint32_t e) {
         const uint32_t u = x[j], v = f.shoup(x[k], __ldg(itw + e));
         x[j] = f.add(u, v);
@@ -209,7 +238,7 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
             x[j + 1] = f.sub(u, v);
         }
         if constexpr (P::R == 2) {
-            const uint2 w1 = __ldg(itw + uint32_t(P::L / 4) * P::S);
+            const uint2 w1 = __ldg(itw + TwLayout::quarter(LG));
 #pragma unroll
             for (int j = 0; j < 8; j += 4) {
                 const uint32_t u0 = x[j], v0 = x[j + 2], u1 = x[j + 1], v1 = f.shoup(x[j + 3], w1);
@@ -224,17 +253,16 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
 #pragma unroll
     for (int k = P::NF - 1; k >= 0; --k) {
         const int d = P::d(k);
-        const uint32_t off = t % d;
-        const uint32_t mult = uint32_t(P::S) << (3 * k);
+        const uint32_t off = t % d, e0 = TwLayout::pass(LG, k) + off;
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) bf(j, j + 1, off * 4 * mult);
+        for (int j = 0; j < 8; j += 2) bf(j, j + 1, e0 + 6 * d);
 #pragma unroll
         for (int j = 0; j < 8; j += 4) {
-            bf(j, j + 2, off * 2 * mult);
-            bf(j + 1, j + 3, (off + d) * 2 * mult);
+            bf(j, j + 2, e0 + 4 * d);
+            bf(j + 1, j + 3, e0 + 5 * d);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf(j, j + 4, (off + d * j) * mult);
+        for (int j = 0; j < 4; ++j) bf(j, j + 4, e0 + d * j);
         if (k > 0) exchange<LG, 1>(xs, sh, d, P::d(k - 1));
     }
 }

@@ -6,8 +6,10 @@
 // The reference rebuilds and copies its twiddle tables on every driver call
 // (getOmega / mkOmegas, cuda/ker-fft-mul.cu.h:191-211; cuda/main.cu:458-470);
 // here they are built once per context and stay in device memory: for each of
-// the five 30-bit primes of the multiplication kernels, w^e and w^-e with
-// their Shoup companions (w = g^((p-1)/4096), the getOmega convention).
+// the five 30-bit primes of the multiplication kernels, the powers of w and of
+// w^-1 (w = g^((p-1)/4096), the getOmega convention) with their Shoup
+// companions, laid out per transform length in the order the passes read
+// them (ntt32::TwLayout; 620 KiB per context).
 #include <cstring>
 #include <vector>
 
@@ -56,8 +58,10 @@ static uint2 shoup_pair(uint64_t c, uint32_t p) {
 }
 
 mi_status ntt_tables_create(NttTables* T) {
-    constexpr int E = ntt32::kTwiddles;
-    std::vector<uint2> h(size_t(10) * E);
+    using ntt32::TwLayout;
+    constexpr int E = ntt32::kTwEntries;
+    std::vector<uint2> h(size_t(10) * E, make_uint2(0, 0));
+    std::vector<uint64_t> pw(ntt32::kTwiddles), ipw(ntt32::kTwiddles);
     NttMulParams& P = T->params;
     std::memset(&P, 0, sizeof(P));
     for (int q = 0; q < 5; ++q) {
@@ -65,11 +69,27 @@ mi_status ntt_tables_create(NttTables* T) {
         const uint64_t w = host_powmod(kNttPrimes[q].g, (uint64_t(p) - 1) >> ntt32::kLgMax, p);  // order 4096
         const uint64_t wi = host_invmod(w, p);
         uint64_t acc = 1, acci = 1;
-        for (int e = 0; e < E; ++e) {
-            h[size_t(2 * q) * E + e] = shoup_pair(acc, p);
-            h[size_t(2 * q + 1) * E + e] = shoup_pair(acci, p);
+        for (int e = 0; e < ntt32::kTwiddles; ++e) {
+            pw[e] = acc;
+            ipw[e] = acci;
             acc = host_mulmod(acc, w, p);
             acci = host_mulmod(acci, wi, p);
+        }
+        // every transform length's sections, in the order its passes read them
+        for (int dir = 0; dir < 2; ++dir) {
+            uint2* out = h.data() + size_t(2 * q + dir) * E;
+            const std::vector<uint64_t>& pows = dir ? ipw : pw;
+            for (int lg = ntt32::kLgMin; lg <= ntt32::kLgMax; ++lg) {
+                uint2* sec = out + TwLayout::base(lg);
+                for (int k = 0; k < TwLayout::nf(lg); ++k) {
+                    const int d = TwLayout::d(lg, k), m = (1 << ntt32::kLgMax) / (8 * d);
+                    uint2* ps = sec + TwLayout::pass(lg, k);
+                    for (int i = 0; i < 4 * d; ++i) ps[i] = shoup_pair(pows[size_t(i) * m], p);
+                    for (int i = 0; i < 2 * d; ++i) ps[4 * d + i] = shoup_pair(pows[size_t(2 * i) * m], p);
+                    for (int i = 0; i < d; ++i) ps[6 * d + i] = shoup_pair(pows[size_t(4 * i) * m], p);
+                }
+                sec[TwLayout::quarter(lg)] = shoup_pair(pows[1024], p);
+            }
         }
         P.p[q] = p;
         uint32_t inv = 1;  // p^-1 mod 2^32 by Newton iteration
@@ -94,6 +114,7 @@ mi_status ntt_tables_create(NttTables* T) {
         P.tw[q] = T->d_tw + size_t(2 * q) * E;
         P.itw[q] = T->d_tw + size_t(2 * q + 1) * E;
     }
+    static_assert(ntt32::kTwEntries == 7936, "twiddle sections of 256..4096-point transforms");
     return MI_OK;
 }
 

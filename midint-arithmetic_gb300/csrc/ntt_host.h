@@ -28,11 +28,11 @@ struct NttMulParams {
     uint2 ka_by_lg[5][5][2];      // a's conversion for L = 2^(8+i): (L^-1, 2^32 L^-1) mod p
     uint2 kb[5][2];               // b's conversion: (2^32, 2^64) mod p
     uint2 garner[10];             // p_k^-1 mod p_i, for i = 1..4, k = 0..i-1
-    const uint2* tw[5];           // (w^e, companion), e < 2048, w of order 4096
-    const uint2* itw[5];          // (w^-e, companion)
+    const uint2* tw[5];           // (w^e, companion), w of order 4096, in ntt32::TwLayout order
+    const uint2* itw[5];          // (w^-e, companion), the same layout
 };
 
-// Device-resident tables of one context (160 KiB) and the parameter block.
+// Device-resident tables of one context (620 KiB) and the parameter block.
 struct NttTables {
     uint2* d_tw = nullptr;
     NttMulParams params{};
