@@ -4,20 +4,27 @@
 // one kernel per operation and compile-time size, cuda/main.cu:661-746.)
 //
 // Stages, all asynchronous on one stream (and so capturable in a CUDA graph):
-//  1. classify: each op gets a size-class key and bumps that key's count;
-//  2. scan (one block): op offsets per key and task offsets per family, with
-//     the keys of each family in descending cost order;
-//  3. scatter: op indices grouped by key;
-//  4. three persistent kernels, one per family, each popping tasks from its
+//  1. classify: each op gets a size-class key; blocks count their keys in
+//     shared memory and add the counts to the global ones;
+//  2. scan (one thread per family): op offsets per key and task offsets per
+//     family, with the keys of each family in descending cost order;
+//  3. scatter: op indices grouped by key (each block reserves its slots of a
+//     key with one atomic);
+//  4. four persistent kernels, one per family, each popping tasks from its
 //     atomic queue:
 //     * NTT products (shorter operand >= the crossover): a task is one CTA of
 //       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh);
-//     * classical rectangular products: a task is one warp = 32/NT products
-//       whose shorter operand fits NT tiles of 8 u32 limbs; the longer one is
-//       consumed in chunks of NT tiles, each chunk a square product
-//       (mul_core.cuh) added into a sliding window whose low half is final --
-//       no padding of either operand to a power of two;
-//     * additions: a task is one CTA of groups sized to max(la, lb).
+//     * classical products with a shorter operand of up to 128 limbs, a task
+//       per warp: comb products when it has at most 8 limbs (each thread
+//       multiplies 16 words of the longer operand by all of it in registers),
+//       otherwise 32/NT products whose shorter operand fits NT tiles of 8 u32
+//       limbs, broadcast to the group, while the longer one streams through
+//       in chunks of NT tiles, each chunk a square product (mul_core.cuh)
+//       added into a sliding window whose low half is final -- no padding of
+//       either operand to a power of two;
+//     * the same chunked products for 129..256 limbs in 64-thread groups;
+//     * additions, a task per warp: lanes of one limb for additions of up to
+//       32 limbs, rows of 32 limbs per warp above that.
 // Within a family the key encodes everything that sets the trip counts of a
 // task, so the groups of a task run in lockstep.
 #include <algorithm>
@@ -37,8 +44,8 @@ namespace rg {
 
 constexpr uint32_t kMaxLimbs = 1024;
 constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11
-constexpr int K_CLS = 6 * 256;   // NT = 1..32 x chunks = 1..256
-constexpr int K_ADD = 10;        // (Q=2, GS=1..32), (Q=4, GS=32..256)
+constexpr int K_CLS = 13;        // NT = 1..16 (one chunk), NT = 32 x chunks = 1..8
+constexpr int K_ADD = 11;        // GS = 1..32 lanes of one limb; one warp over 2..32 rows of 32 limbs
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
 constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
 constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_CMB = KEY_CLS + K_CLS, KEY_ADD = KEY_CMB + K_CMB,
@@ -46,6 +53,7 @@ constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_CMB = KEY_CLS + K_CLS, KEY_ADD =
 constexpr int K = KEY_C64 + K_C64;
 constexpr int NFAM = 4;          // families: NTT, classical in a warp, additions, classical in 64 threads
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
+constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
 constexpr int C64_GROUP_WORDS = 512 + 512 + 64 * classic::PER_T;  // the same for one 64-thread group
 
@@ -83,8 +91,8 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
     if (la == 0 || lb == 0 || la > kMaxLimbs || lb > kMaxLimbs) return KEY_INVALID;
     if (op.kind == MI_OP_ADD) {
         const uint32_t m = max(la, lb);
-        if (m <= 64) return KEY_ADD + ceil_log2((m + 1) / 2);
-        return KEY_ADD + 6 + ceil_log2((m + 3) / 4) - 5;
+        if (m <= 32) return KEY_ADD + ceil_log2(m);       // groups of 1..32 lanes, one limb each
+        return KEY_ADD + 5 + ceil_log2((m + 31) / 32);    // a warp over 2, 4, 8, 16, 32 rows
     }
     if (op.kind == MI_OP_MUL) {
         const uint32_t s = min(la, lb), l = max(la, lb);
@@ -105,101 +113,114 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
         // longer operand up to one warp, and never narrower than the shorter
         const uint32_t nbs = (2 * s + 7) / 8, nbl = (2 * l + 7) / 8;
         const uint32_t ntl = ceil_log2(max(nbs, min(nbl, 32u)));  // NT = 2^ntl <= 32
-        const uint32_t nt = 1u << ntl;
-        const uint32_t chunks = (nbl + nt - 1) / nt;
-        return KEY_CLS + ntl * 256 + (chunks - 1);
+        if (ntl < 5) return KEY_CLS + ntl;  // NT >= nbl: one chunk
+        return KEY_CLS + 5 + (nbl + 31) / 32 - 1;  // NT = 32, nbl <= 256: 1..8 chunks
     }
     return KEY_INVALID;
 }
 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
     if (key < KEY_CLS) return 2048u >> (8 + key);                    // NTT: 256 threads / (L/8)
-    if (key < KEY_CMB) return 32u >> ((key - KEY_CLS) / 256);        // classical: one warp
+    if (key < KEY_CMB) {                                              // classical: one warp
+        const uint32_t k = key - KEY_CLS;
+        return k < 5 ? 32u >> k : 1u;
+    }
     if (key < KEY_ADD) return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;  // comb: 32 / group
     if (key >= KEY_C64) return 4u;                                    // classical: 256 threads / 64
-    const uint32_t k = key - KEY_ADD;                                 // add: 256 threads / GS
-    const uint32_t gs = k < 6 ? (1u << k) : (32u << (k - 6));
-    return 256u / gs;
+    const uint32_t k = key - KEY_ADD;                                 // add: one warp
+    return k < 6 ? 32u >> k : kAddRowOps;
 }
 
-__global__ void k_classify(const mi_op* __restrict__ ops, uint32_t n, uint32_t* __restrict__ scr, uint32_t ntt_min) {
-    uint32_t* counts = scr + Scratch::COUNTS;
+// Binning.  Blocks of classify and scatter own the same contiguous ranges of
+// kBinRange ops and count their keys in shared memory, so the global counters
+// take one atomic per (block, key) instead of one per op.
+constexpr uint32_t kBinRange = 1024;
+static_assert(K <= 256, "one shared counter per thread");
+
+__global__ void __launch_bounds__(256) k_classify(const mi_op* __restrict__ ops, uint32_t n,
+                                                  uint32_t* __restrict__ scr, uint32_t ntt_min) {
+    __shared__ uint32_t hist[K + 1];  // the keys, then the invalid ops
+    for (int k = threadIdx.x; k <= K; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
     uint32_t* keys = scr + Scratch::KEYS;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t lo = blockIdx.x * kBinRange, hi = min(n, lo + kBinRange);
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const uint32_t key = classify(ops[i], ntt_min);
         keys[i] = key;
-        if (key == KEY_INVALID)
-            atomicAdd(scr + Scratch::INVALID, 1u);
-        else
-            atomicAdd(counts + key, 1u);
-    }
-}
-
-// One block of 1024 threads: exclusive scans over the keys in c_order.
-__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ scr) {
-    constexpr int N = 2048;
-    __shared__ uint32_t s_ops[N], s_tasks[N];
-    const uint32_t* counts = scr + Scratch::COUNTS;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        uint32_t c = 0, tk = 0;
-        if (i < K) {
-            const uint32_t key = c_order[i];
-            c = counts[key];
-            const uint32_t opt = ops_per_task(key);
-            tk = (c + opt - 1) / opt;
-        }
-        s_ops[i] = c;
-        s_tasks[i] = tk;
-        if (i < K) scr[Scratch::CURSORS + i] = 0;
+        atomicAdd(&hist[key == KEY_INVALID ? K : key], 1u);
     }
     __syncthreads();
-    // inclusive Hillis-Steele scans of both arrays
-    for (int d = 1; d < N; d <<= 1) {
-        uint32_t v0[2], v1[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int i = threadIdx.x + h * 1024;
-            v0[h] = s_ops[i] + (i >= d ? s_ops[i - d] : 0);
-            v1[h] = s_tasks[i] + (i >= d ? s_tasks[i - d] : 0);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int i = threadIdx.x + h * 1024;
-            s_ops[i] = v0[h];
-            s_tasks[i] = v1[h];
-        }
-        __syncthreads();
+    if (threadIdx.x < K && hist[threadIdx.x]) atomicAdd(scr + Scratch::COUNTS + threadIdx.x, hist[threadIdx.x]);
+    if (threadIdx.x == K && hist[K]) atomicAdd(scr + Scratch::INVALID, hist[K]);
+}
+
+// First key of family f (f = NFAM: the end of the key space).
+__host__ __device__ constexpr int fam_base(int f) {
+    return f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : K)));
+}
+static_assert(fam_base(1) - fam_base(0) <= 32 && fam_base(2) - fam_base(1) <= 32 &&
+                  fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32,
+              "a family's keys fit one warp");
+
+// One warp per family scans its keys in c_order (shuffle scans): op offsets
+// by key (global over the families), task starts by order position with one
+// sentinel per family, task counts; the queues restart at 0.
+__global__ void __launch_bounds__(32 * NFAM) k_scan(uint32_t* __restrict__ scr) {
+    __shared__ uint32_t fam_ops[NFAM];
+    const int f = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = fam_base(f), nk = fam_base(f + 1) - base;
+    uint32_t key = 0, c = 0, tk = 0;
+    if (lane < nk) {
+        key = c_order[base + lane];
+        c = scr[Scratch::COUNTS + key];
+        const uint32_t opt = ops_per_task(key);
+        tk = (c + opt - 1) / opt;
     }
-    // op offsets (exclusive, global over the ordered keys) and per-family task starts
-    const int fam_start[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, K};  // family 1 holds the comb keys too
-    for (int i = threadIdx.x; i < K; i += blockDim.x) {
-        const uint32_t key = c_order[i];
-        scr[Scratch::OPOFF + key] = i ? s_ops[i - 1] : 0;
-        const int f = i < KEY_CLS ? 0 : (i < KEY_ADD ? 1 : (i < KEY_C64 ? 2 : 3));
-        const int base = fam_start[f];
-        const uint32_t before = base ? s_tasks[base - 1] : 0;
-        scr[Scratch::TS + f + i] = (i ? s_tasks[i - 1] : 0) - before;
+    uint32_t ci = c, ti = tk;  // inclusive scans
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t u = __shfl_up_sync(MI_FULL_MASK, ci, d), v = __shfl_up_sync(MI_FULL_MASK, ti, d);
+        if (lane >= d) {
+            ci += u;
+            ti += v;
+        }
     }
-    if (threadIdx.x < NFAM) {
-        const int f = threadIdx.x;
-        const int base = fam_start[f], end = fam_start[f + 1];
-        const uint32_t before = base ? s_tasks[base - 1] : 0;
-        const uint32_t total = s_tasks[end - 1] - before;
-        scr[Scratch::TS + f + end] = total;  // sentinel
-        scr[Scratch::NTASKS + f] = total;
+    if (lane == 31) fam_ops[f] = ci;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int g = 0; g < f; ++g) before += fam_ops[g];
+    if (lane < nk) {
+        scr[Scratch::OPOFF + key] = before + ci - c;
+        scr[Scratch::TS + f + base + lane] = ti - tk;
+    }
+    if (lane == 31) {
+        scr[Scratch::TS + f + base + nk] = ti;  // sentinel
+        scr[Scratch::NTASKS + f] = ti;
         scr[Scratch::QUEUE + f] = 0;
     }
 }
 
-__global__ void k_scatter(uint32_t n, uint32_t* __restrict__ scr) {
+__global__ void __launch_bounds__(256) k_scatter(uint32_t n, uint32_t* __restrict__ scr) {
+    __shared__ uint32_t hist[K], base[K];
+    for (int k = threadIdx.x; k < K; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
     const uint32_t* keys = scr + Scratch::KEYS;
     uint32_t* sorted = scr + Scratch::sorted(n);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t lo = blockIdx.x * kBinRange, hi = min(n, lo + kBinRange);
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const uint32_t key = keys[i];
-        if (key == KEY_INVALID) continue;
-        const uint32_t pos = scr[Scratch::OPOFF + key] + atomicAdd(scr + Scratch::CURSORS + key, 1u);
-        sorted[pos] = i;
+        if (key != KEY_INVALID) atomicAdd(&hist[key], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {  // this block's slots of each key
+        const uint32_t k = threadIdx.x;
+        if (hist[k]) base[k] = scr[Scratch::OPOFF + k] + atomicAdd(scr + Scratch::CURSORS + k, hist[k]);
+        hist[k] = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const uint32_t key = keys[i];
+        if (key != KEY_INVALID) sorted[base[key] + atomicAdd(&hist[key], 1u)] = i;
     }
 }
 
@@ -298,7 +319,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     const uint32_t g = lane / NT, t = lane % NT;
     const bool valid = g < tk.count;
     if (!WIDE && !valid) return;  // warp groups synchronise only among their own lanes
-    const uint32_t chunks = WIDE ? tk.key - KEY_C64 + 1 : (tk.key - KEY_CLS) % 256 + 1;
+    const uint32_t chunks = WIDE ? tk.key - KEY_C64 + 1 : (tk.key - KEY_CLS < 5 ? 1u : tk.key - KEY_CLS - 4);
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     mi_op op{};
     if (valid) op = P.ops[sorted[tk.first + g]];
@@ -474,7 +495,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
             __syncwarp();
             continue;
         }
-        switch ((tk.key - KEY_CLS) / 256) {
+        switch (min(tk.key - KEY_CLS, 5u)) {
             case 0: classic_task<1>(P, tk, wsm, nullptr); break;
             case 1: classic_task<2>(P, tk, wsm, nullptr); break;
             case 2: classic_task<4>(P, tk, wsm, nullptr); break;
@@ -505,69 +526,90 @@ __global__ void __launch_bounds__(256, 2) k_rg_c64(Params P) {
 }
 
 // --- addition family -------------------------------------------------------------
+//
+// Warp tasks.  Additions of at most 32 limbs: groups of GS = pow2ceil(m)
+// lanes, one limb per lane, 32/GS additions per task, one carry-lookahead
+// pass per group.  Longer additions: one warp per addition, lane i of row r
+// owning limb 32r + i, so every load and store of the warp is 256 contiguous
+// bytes; rows are loaded eight at a time and resolved in order, each row's
+// carry-out entering the next row's lookahead.
 
-template <int Q, int GS>
-__device__ __forceinline__ void add_task(const Params& P, const Task& tk, uint32_t* scr_warp) {
-    const uint32_t g = threadIdx.x / GS, t = threadIdx.x % GS;
-    const bool valid = g < tk.count;
+template <int GS>
+__device__ __forceinline__ void add_short(const Params& P, const Task& tk) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t g = lane / GS, t = lane % GS;
+    if (g >= tk.count) return;  // groups vote only among their own lanes
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
-    const uint32_t idx = valid ? sorted[tk.first + g] : 0;
-    const mi_op op = valid ? P.ops[idx] : mi_op{};
+    const uint32_t idx = sorted[tk.first + g];
+    const mi_op op = P.ops[idx];
     const uint32_t m = max(op.la, op.lb);
-    const uint64_t* ar = P.in + op.a_off;
-    const uint64_t* br = P.in + op.b_off;
-    const uint32_t start = t * Q;
-    uint64_t x[Q], y[Q], s[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        x[q] = (valid && start + q < op.la) ? __ldcs(reinterpret_cast<const unsigned long long*>(ar + start + q)) : 0;
-        y[q] = (valid && start + q < op.lb) ? __ldcs(reinterpret_cast<const unsigned long long*>(br + start + q)) : 0;
-    }
-    bool gg, pp;
-    chunk_add<uint64_t, Q>(x, y, s, gg, pp);
+    const uint64_t x = t < op.la ? __ldcs(reinterpret_cast<const unsigned long long*>(P.in + op.a_off + t)) : 0;
+    const uint64_t y = t < op.lb ? __ldcs(reinterpret_cast<const unsigned long long*>(P.in + op.b_off + t)) : 0;
+    uint64_t s = x + y;
     uint32_t gc;
-    const uint32_t cin = group_carry<GS>(gg, pp, 0u, &gc, scr_warp);
-    chunk_inc<uint64_t, Q>(s, cin);
-    if (!valid) return;
-    uint64_t* rr = P.out + op.r_off;
-#pragma unroll
-    for (int q = 0; q < Q; ++q)
-        if (start + q < m) rr[start + q] = s[q];
+    s += group_carry<GS>(s < x, s == ~0ull, 0u, &gc, nullptr);
+    if (t < m) P.out[op.r_off + t] = s;
     if (P.carry != nullptr) {
-        if (m < uint32_t(GS * Q)) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-                if (start + q == m) P.carry[idx] = uint8_t(s[q]);
-        } else if (t == GS - 1) {
-            P.carry[idx] = uint8_t(gc);
-        }
+        if (t == m) P.carry[idx] = uint8_t(s);                     // limb m holds the carry-out
+        else if (m == GS && t == GS - 1) P.carry[idx] = uint8_t(gc);
     }
 }
 
-__global__ void __launch_bounds__(256, 2) k_rg_add(Params P) {
-    __shared__ uint32_t scr_warp[8];
-    __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
+__device__ __forceinline__ void add_rows(const Params& P, const Task& tk) {
+    constexpr int RB = 8;  // rows in flight per batch
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    for (uint32_t o = 0; o < tk.count; ++o) {
+        const uint32_t idx = sorted[tk.first + o];
+        const mi_op op = P.ops[idx];
+        const uint32_t m = max(op.la, op.lb), rows = (m + 31) / 32;
+        const unsigned long long* ar = reinterpret_cast<const unsigned long long*>(P.in + op.a_off);
+        const unsigned long long* br = reinterpret_cast<const unsigned long long*>(P.in + op.b_off);
+        uint64_t* rr = P.out + op.r_off;
+        uint32_t carry = 0;
+        for (uint32_t r0 = 0; r0 < rows; r0 += RB) {
+            uint64_t x[RB], y[RB];
+#pragma unroll
+            for (int r = 0; r < RB; ++r) {
+                const uint32_t i = (r0 + r) * 32 + lane;
+                x[r] = i < op.la ? __ldcs(ar + i) : 0;
+                y[r] = i < op.lb ? __ldcs(br + i) : 0;
+            }
+#pragma unroll
+            for (int r = 0; r < RB; ++r) {
+                if (r0 + r >= rows) break;  // uniform across the warp
+                const uint32_t i = (r0 + r) * 32 + lane;
+                uint64_t s = x[r] + y[r];
+                uint32_t gc;
+                s += group_carry<32>(s < x[r], s == ~0ull, carry, &gc, nullptr);
+                carry = gc;
+                if (i < m) rr[i] = s;
+                else if (i == m && P.carry != nullptr) P.carry[idx] = uint8_t(s);  // limb m: the carry-out
+            }
+        }
+        if (P.carry != nullptr && m % 32 == 0 && lane == 0) P.carry[idx] = uint8_t(carry);
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) k_rg_add(Params P) {
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 2];
-    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
-    __syncthreads();
-    for (uint32_t it = 0;; ++it) {
-        const uint32_t t = s_task[it & 1];
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
+        t = __shfl_sync(MI_FULL_MASK, t, 0);
         if (t >= ntasks) break;
-        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
         const Task tk = decode(P.scr, 2, t);
         switch (tk.key - KEY_ADD) {
-            case 0: add_task<2, 1>(P, tk, scr_warp); break;
-            case 1: add_task<2, 2>(P, tk, scr_warp); break;
-            case 2: add_task<2, 4>(P, tk, scr_warp); break;
-            case 3: add_task<2, 8>(P, tk, scr_warp); break;
-            case 4: add_task<2, 16>(P, tk, scr_warp); break;
-            case 5: add_task<2, 32>(P, tk, scr_warp); break;
-            case 6: add_task<4, 32>(P, tk, scr_warp); break;
-            case 7: add_task<4, 64>(P, tk, scr_warp); break;
-            case 8: add_task<4, 128>(P, tk, scr_warp); break;
-            default: add_task<4, 256>(P, tk, scr_warp); break;
+            case 0: add_short<1>(P, tk); break;
+            case 1: add_short<2>(P, tk); break;
+            case 2: add_short<4>(P, tk); break;
+            case 3: add_short<8>(P, tk); break;
+            case 4: add_short<16>(P, tk); break;
+            case 5: add_short<32>(P, tk); break;
+            default: add_rows(P, tk); break;
         }
-        __syncthreads();  // the next index is visible; this one is read by all
+        __syncwarp();
     }
 }
 
@@ -589,17 +631,9 @@ mi_status init_device() {
     // keys of each family in descending cost
     std::vector<uint16_t> order(K);
     for (int k = 0; k < K_NTT; ++k) order[KEY_NTT + k] = uint16_t(KEY_NTT + (K_NTT - 1 - k));
-    std::vector<int> cls(K_CLS);
-    for (int k = 0; k < K_CLS; ++k) cls[k] = k;
-    // Group size first, ascending, then chunks, descending: consecutive tasks
-    // run the same code (one inlined square product per group size, so
-    // warps of an SM share their instructions), the long chunk chains of
-    // small groups -- latency-bound, one operand load per chunk -- start
-    // first, and the queue ends with the shortest tasks of the largest groups.
-    std::stable_sort(cls.begin(), cls.end(), [](int x, int y) {
-        return x / 256 != y / 256 ? x / 256 < y / 256 : x % 256 > y % 256;
-    });
-    for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + cls[k]);
+    // classical keys by descending cost: 32-thread groups from 8 chunks down
+    // to 1, then groups of 16, 8, 4, 2, 1 threads (one chunk each)
+    for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + (K_CLS - 1 - k));
     // comb keys after them, the most passes first
     const int comb[K_CMB] = {6, 5, 4, 3, 2, 1, 0};
     for (int k = 0; k < K_CMB; ++k) order[KEY_CMB + k] = uint16_t(KEY_CMB + comb[k]);
@@ -641,9 +675,9 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     P.ntt_min = ntt_min < 1 ? 1 : (ntt_min > 257 ? 257 : ntt_min);
     P.ntt = ctx->ntt.params;
     MI_CUDA_TRY(cudaMemsetAsync(P.scr, 0, (Scratch::KEYS) * 4, st));
-    const uint32_t blocks = std::min<uint32_t>((n_ops + 255) / 256, uint32_t(sm_count() * 8));
+    const uint32_t blocks = (n_ops + kBinRange - 1) / kBinRange;
     k_classify<<<blocks, 256, 0, st>>>(ops, n_ops, P.scr, P.ntt_min);
-    k_scan<<<1, 1024, 0, st>>>(P.scr);
+    k_scan<<<1, 32 * NFAM, 0, st>>>(P.scr);  // the cursors were zeroed with the counts
     k_scatter<<<blocks, 256, 0, st>>>(n_ops, P.scr);
     k_rg_ntt<<<persistent_grid((const void*)k_rg_ntt, kNttSmem), 256, kNttSmem, st>>>(P);
     k_rg_classic<<<persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st>>>(P);

@@ -10,10 +10,10 @@ namespace mi {
 namespace tuned {
 
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
-constexpr uint32_t kPlainNttMin = 256;
+constexpr uint32_t kPlainNttMin = 160;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
-constexpr uint32_t kRaggedNttMin = 128;
+constexpr uint32_t kRaggedNttMin = 96;
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32, 32, 64, 64};
