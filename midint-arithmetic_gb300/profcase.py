@@ -15,6 +15,10 @@ when --warmup 1) with seeded inputs already resident on the device:
   ragged_bands  the --ragged-ops list cut into its additions and its products
           by shorter-operand band, each band timed alone as its own captured
           ragged run (CUDA events over 10 replays after 3) and printed as JSON
+  wide_variants  additions of 16 pairs x 2^21 u64 limbs with no all-ones pair,
+          every 8th pair all-ones + 1, and every pair all-ones + 1 (the
+          carry runs through every tile), each timed with CUDA events over
+          10 launches after 3 and printed as JSON with GB/s
 
 Usage: python midint-arithmetic_gb300/profcase.py [--ops add,mul,...] [--warmup 0|1]
 """
@@ -106,8 +110,40 @@ def main():
     torch.cuda.synchronize()
     if "ragged_bands" in ops:
         print(json.dumps(ragged_bands(ctx, dev, sp, args.ragged_ops), indent=1))
+    if "wide_variants" in ops:
+        print(json.dumps(wide_variants(ctx, dev, sp), indent=1))
     ctx.close()
     print("profcase: ran", ",".join(ops))
+
+
+def wide_variants(ctx, dev, sp) -> dict:
+    """16 x 2^21-limb additions with 0, 1/8 and all pairs carrying through."""
+    import torch
+
+    import workloads
+
+    n, m = 16, 1 << 21
+    res = {}
+    for name, worst in (("uniform", 0), ("every 8th all-ones", 8), ("all all-ones", 1)):
+        a, b = workloads.add_pairs(n=n, m=m, worst_every=worst)
+        da = torch.from_numpy(a.view(np.int64)).to(dev)
+        db = torch.from_numpy(b.view(np.int64)).to(dev)
+        dr = torch.empty_like(da)
+        dc = torch.empty(n, dtype=torch.uint8, device=dev)
+        for _ in range(3):
+            ctx.add(da, db, dr, n, m, carry=dc, stream=sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ctx.add(da, db, dr, n, m, carry=dc, stream=sp)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        res[name] = {"ms": ms, "GB/s": (3 * n * m * 8 + n) / ms / 1e6}
+        del da, db, dr
+        torch.cuda.empty_cache()
+    res["device_status"] = ctx.device_status()
+    return res
 
 
 # (name, kind, lowest shorter-operand limbs, highest) of each band
