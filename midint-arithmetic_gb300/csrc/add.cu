@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
     const uint32_t t = threadIdx.x % GS;
     const uint32_t start = t * Q;
     const uint64_t stride = uint64_t(gridDim.x) * IPB;
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
     // Uniform trip count per block: group_carry synchronises the block for GS > 32.
     for (uint64_t base = uint64_t(blockIdx.x) * IPB; base < n; base += stride) {
         const uint64_t inst = base + grp;
@@ -384,8 +386,7 @@ mi_status launch_one(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, u
     // Enough blocks for full residency several times over; the kernel strides.
     const uint64_t cap = uint64_t(sm_count()) * 64;
     if (blocks > cap) blocks = cap;
-    k_add<L, Q, GS, VEC, OP><<<dim3(uint32_t(blocks)), dim3(BLOCK), 0, st>>>(a, b, r, carry, n, m);
-    MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(launch_pdl(k_add<L, Q, GS, VEC, OP>, dim3(uint32_t(blocks)), dim3(BLOCK), 0, st, a, b, r, carry, n, m));
     return MI_OK;
 }
 

@@ -60,6 +60,32 @@ inline bool any_overlap(const void* p, size_t bytes, const void* q, size_t bytes
     return a0 < b0 + bytes2 && b0 < a0 + bytes;
 }
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may have
+// its blocks made resident while the previous kernel of the stream is still
+// finishing; it must call pdl_wait() before its first global-memory access,
+// which returns once that kernel has completed and its writes are visible.
+// pdl_trigger() lets the next kernel's blocks start the same way once every
+// block of this grid has called it.  The launch latency between back-to-back
+// kernels then overlaps the previous kernel's tail.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // ---------------------------------------------------------------------------
 // Device primitives: 32-bit carry chains in PTX.  Each wrapper is one PTX
 // instruction in its own `asm volatile`, so the compiler keeps them in program

@@ -51,6 +51,8 @@ __global__ void k_import(const typename Word<SIZE>::T* __restrict__ src, uint64_
                          uint32_t words, uint32_t limbs, int most_first, int big) {
     using W = Word<SIZE>;
     constexpr uint32_t PER = 8 / SIZE;  // words per limb
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
     for (uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
          idx += uint64_t(gridDim.x) * blockDim.x) {
         const uint64_t i = idx / limbs;
@@ -75,6 +77,8 @@ __global__ void k_export(const uint64_t* __restrict__ src, typename Word<SIZE>::
                          uint32_t limbs, uint32_t words, int most_first, int big) {
     using W = Word<SIZE>;
     constexpr uint32_t PER = 8 / SIZE;
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
     for (uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
          idx += uint64_t(gridDim.x) * blockDim.x) {
         const uint64_t i = idx / words;
@@ -93,6 +97,8 @@ __global__ void k_count_words(const uint64_t* __restrict__ src, uint32_t* __rest
                               uint32_t limbs, uint32_t size) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t warps = uint64_t(gridDim.x) * (blockDim.x / 32);
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
     for (uint64_t i = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; i < n; i += warps) {
         const uint64_t* row = src + i * limbs;
         uint32_t count = 0;
@@ -126,14 +132,15 @@ mi_status launch_import(const void* src, uint64_t* dst, uint32_t n, uint32_t wor
     const uint64_t total = uint64_t(n) * limbs;
     const int mf = order > 0, big = endian > 0;
     const uint32_t g = grid_for(total);
+    cudaError_t e = cudaSuccess;
     switch (size) {
-        case 1: k_import<1><<<g, 256, 0, st>>>(static_cast<const uint8_t*>(src), dst, total, words, limbs, mf, big); break;
-        case 2: k_import<2><<<g, 256, 0, st>>>(static_cast<const uint16_t*>(src), dst, total, words, limbs, mf, big); break;
-        case 4: k_import<4><<<g, 256, 0, st>>>(static_cast<const uint32_t*>(src), dst, total, words, limbs, mf, big); break;
-        case 8: k_import<8><<<g, 256, 0, st>>>(static_cast<const uint64_t*>(src), dst, total, words, limbs, mf, big); break;
+        case 1: e = launch_pdl(k_import<1>, g, 256, 0, st, static_cast<const uint8_t*>(src), dst, total, words, limbs, mf, big); break;
+        case 2: e = launch_pdl(k_import<2>, g, 256, 0, st, static_cast<const uint16_t*>(src), dst, total, words, limbs, mf, big); break;
+        case 4: e = launch_pdl(k_import<4>, g, 256, 0, st, static_cast<const uint32_t*>(src), dst, total, words, limbs, mf, big); break;
+        case 8: e = launch_pdl(k_import<8>, g, 256, 0, st, static_cast<const uint64_t*>(src), dst, total, words, limbs, mf, big); break;
         default: return set_error(MI_EINVAL, "import: word size %u not 1, 2, 4 or 8", size);
     }
-    MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(e);
     return MI_OK;
 }
 
@@ -142,17 +149,17 @@ mi_status launch_export(const uint64_t* src, void* dst, uint32_t n, uint32_t lim
     const uint64_t total = uint64_t(n) * words;
     const int mf = order > 0, big = endian > 0;
     const uint32_t g = grid_for(total);
+    cudaError_t e = cudaSuccess;
     switch (size) {
-        case 1: k_export<1><<<g, 256, 0, st>>>(src, static_cast<uint8_t*>(dst), total, limbs, words, mf, big); break;
-        case 2: k_export<2><<<g, 256, 0, st>>>(src, static_cast<uint16_t*>(dst), total, limbs, words, mf, big); break;
-        case 4: k_export<4><<<g, 256, 0, st>>>(src, static_cast<uint32_t*>(dst), total, limbs, words, mf, big); break;
-        case 8: k_export<8><<<g, 256, 0, st>>>(src, static_cast<uint64_t*>(dst), total, limbs, words, mf, big); break;
+        case 1: e = launch_pdl(k_export<1>, g, 256, 0, st, src, static_cast<uint8_t*>(dst), total, limbs, words, mf, big); break;
+        case 2: e = launch_pdl(k_export<2>, g, 256, 0, st, src, static_cast<uint16_t*>(dst), total, limbs, words, mf, big); break;
+        case 4: e = launch_pdl(k_export<4>, g, 256, 0, st, src, static_cast<uint32_t*>(dst), total, limbs, words, mf, big); break;
+        case 8: e = launch_pdl(k_export<8>, g, 256, 0, st, src, static_cast<uint64_t*>(dst), total, limbs, words, mf, big); break;
         default: return set_error(MI_EINVAL, "export: word size %u not 1, 2, 4 or 8", size);
     }
-    MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(e);
     if (counts != nullptr) {
-        k_count_words<<<grid_for(uint64_t(n) * 32), 256, 0, st>>>(src, counts, n, limbs, size);
-        MI_CUDA_TRY(cudaGetLastError());
+        MI_CUDA_TRY(launch_pdl(k_count_words, grid_for(uint64_t(n) * 32), 256, 0, st, src, counts, n, limbs, size));
     }
     return MI_OK;
 }

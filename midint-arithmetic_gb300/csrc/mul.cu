@@ -47,6 +47,8 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 
     const uint32_t rlen = full ? 2 * n32 : n32;
     const uint32_t nb = (n32 + T - 1) / T;  // blocks holding limbs; the rest of the NT are zero padding
     const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
 
     // Every group of a block runs the same trip count (wide groups synchronise
     // the whole block).
@@ -86,8 +88,7 @@ mi_status launch_nt(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t 
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
     const uint64_t cap = uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;
-    kern<<<dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st>>>(a, b, r, n, n32, full);
-    MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(launch_pdl(kern, dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st, a, b, r, n, n32, full));
     return MI_OK;
 }
 

@@ -20,8 +20,9 @@ struct LoShape {
 
 using LoKernel = void (*)(const uint32_t*, const uint32_t*, uint32_t*, uint32_t, uint32_t);
 
-// Launches kern (a low-half kernel with NH threads per instance); attr_done is
-// the caller's per-device flag for the shared-memory opt-in.
+// Launches kern (a low-half kernel with NH threads per instance, which starts
+// with pdl_wait) with launch_pdl; attr_done is the caller's per-device flag
+// for the shared-memory opt-in.
 template <int NH>
 mi_status launch_lo(LoKernel kern, bool* attr_done, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n,
                     uint32_t n32, cudaStream_t st) {
@@ -35,8 +36,7 @@ mi_status launch_lo(LoKernel kern, bool* attr_done, const uint32_t* a, const uin
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
     const uint64_t cap = uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;
-    kern<<<dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st>>>(a, b, r, n, n32);
-    MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(launch_pdl(kern, dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st, a, b, r, n, n32));
     return MI_OK;
 }
 

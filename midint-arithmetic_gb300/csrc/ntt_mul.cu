@@ -69,6 +69,11 @@ mi_status launch_lg(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t 
     MI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::NT, S::SMEM));
     uint64_t blocks = uint64_t(sm_count()) * (per_sm > 0 ? per_sm : 1);
     if (blocks > n) blocks = n;
+    // A plain launch: the grid is persistent with a fixed stride over the
+    // instances, and a programmatic dependent launch, whose blocks become
+    // resident one by one during the previous launch's tail, put the blocks
+    // with one instance more on the same SMs (measured 0.108 ms against
+    // 0.0996 ms per 1024 x 65536-bit batch).
     kern<<<dim3(uint32_t(blocks)), dim3(S::NT), S::SMEM, st>>>(a, b, r, n, m, rlen, P);
     MI_CUDA_TRY(cudaGetLastError());
     return MI_OK;

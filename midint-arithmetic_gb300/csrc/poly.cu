@@ -90,6 +90,8 @@ __global__ void __launch_bounds__(NH > 256 ? NH : 256, 2)
     uint32_t* scr = sA;
     const uint32_t nb = (n32 + T - 1) / T;
     const uint64_t stride = uint64_t(gridDim.x) * S::IPB;
+    pdl_wait();  // launched with launch_pdl
+    pdl_trigger();
     for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride) {
         const uint64_t inst = base + grp;
         const bool valid = inst < n;
