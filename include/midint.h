@@ -117,9 +117,15 @@ enum {
                                   * tests: the first tile of every instance
                                   * never publishes its carry, so the waits of
                                   * its successors run out (bounded) */
-    MI_TUNE_WIDE_ROUND_TILES = 7 /* cls ignored; 1..65536: tiles (2048 u64 limbs
-                                  * each) per multi-block launch; an instance
-                                  * may not need more (default 65536) */
+    MI_TUNE_WIDE_ROUND_TILES = 7, /* cls ignored; 1..65536: tiles (2048 u64 limbs
+                                   * each) per multi-block launch; an instance
+                                   * may not need more (default 65536) */
+    MI_TUNE_HOST_ZC_BLOCKS = 8    /* cls as for MI_TUNE_HOST_CHUNKS; value 0..3:
+                                   * with zero-copy mode 1, at most this many
+                                   * blocks per SM for the classical
+                                   * multiplication kernel (0: as many as fit).
+                                   * Fewer resident blocks make the first
+                                   * results leave over the host link sooner */
 };
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
 

@@ -151,12 +151,13 @@ def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
     return pick, {"ops": n_ops, "candidates": record}
 
 
-def tune_host(ctx) -> tuple[list[int], list[int], dict]:
+def tune_host(ctx) -> tuple[list[int], list[int], list[int], dict]:
     """Host-buffer calls on pinned buffers, wall-clock per call, for every chunk
     count and with zero-copy: class 0 on the addition batch (65536 x 64 u64
     limbs, with carries), class 1 on the classical multiplication batch (16384
     x 128 u64 limbs, full products).  Each class takes its fastest chunk count
-    and zero-copy where it beats that."""
+    and zero-copy where it beats that; mode 1 is timed with every cap on the
+    product kernel's resident blocks per SM (0 = none)."""
     import time
 
     import torch
@@ -180,13 +181,17 @@ def tune_host(ctx) -> tuple[list[int], list[int], dict]:
             fn()
         return (time.perf_counter() - t0) / reps * 1e3
 
-    record, chunks, zero_copy = {}, [], []
+    record, chunks, zero_copy, zc_blocks = {}, [], [], []
     for cls, name in ((0, "add"), (1, "mul")):
         cands = {}
-        for zc, ch in [(0, c) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1)] + [(2, c) for c in (2, 3, 4, 6, 8, 12)]:
+        grid = ([(0, c, 0) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1, k) for k in (0, 1, 2, 3)]
+                + [(2, c, 0) for c in (2, 3, 4, 6, 8, 12)])
+        for zc, ch, kb in grid:
             ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
             ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
-            cands[f"zero_copy={zc},chunks={ch}"] = {"zero_copy": zc, "chunks": ch, "ms": wall(calls[cls])}
+            ctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, cls, kb)
+            cands[f"zero_copy={zc},chunks={ch},zc_blocks={kb}"] = {"zero_copy": zc, "chunks": ch, "zc_blocks": kb,
+                                                                  "ms": wall(calls[cls])}
         # the pipeline's chunk count also serves callers whose buffers are
         # not pinned, so it is the best copy pipeline's unless mode 2 (which
         # chunks the same way) wins
@@ -194,12 +199,15 @@ def tune_host(ctx) -> tuple[list[int], list[int], dict]:
         best = min(cands.values(), key=lambda v: v["ms"])
         zc = best["zero_copy"]
         ch = best["chunks"] if zc == 2 else best_copy["chunks"]
+        kb = best["zc_blocks"] if zc == 1 else 0
         ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
         ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
+        ctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, cls, kb)
         chunks.append(ch)
         zero_copy.append(zc)
-        record[name] = {"candidates": cands, "pick": {"chunks": ch, "zero_copy": zc}}
-    return chunks, zero_copy, record
+        zc_blocks.append(kb)
+        record[name] = {"candidates": cands, "pick": {"chunks": ch, "zero_copy": zc, "zc_blocks": kb}}
+    return chunks, zero_copy, zc_blocks, record
 
 
 HEADER = """// tuning_table.h -- defaults of the tunable launch choices, written by
@@ -227,6 +235,9 @@ constexpr uint8_t kAddThreadBytes[13] = {{{add}}};
 // read the operands in place and the results are copied out).
 constexpr uint32_t kHostChunks[2] = {{{chunks}}};
 constexpr uint32_t kHostZeroCopy[2] = {{{zero_copy}}};
+// Zero-copy mode 1: resident blocks per SM of the classical product kernel
+// (0: as many as fit).
+constexpr uint32_t kHostZcBlocks[2] = {{{zc_blocks}}};
 
 }}  // namespace tuned
 }}  // namespace mi
@@ -255,6 +266,7 @@ def main():
     picks = dict(old["picks"])
     picks.setdefault("host_chunks", [4, 6])
     picks.setdefault("host_zero_copy", [0, 1])
+    picks.setdefault("host_zc_blocks", [0, 0])
     record = {k: old.get(k) for k in ("add", "plain_crossover", "ragged_crossover", "host")}
     if "add" in only:
         picks["add_thread_bytes"], record["add"] = tune_add(ctx, stream, dev)
@@ -263,13 +275,14 @@ def main():
     if "ragged" in only:
         picks["ragged_ntt_min"], record["ragged_crossover"] = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
     if "host" in only:
-        picks["host_chunks"], picks["host_zero_copy"], record["host"] = tune_host(ctx)
+        picks["host_chunks"], picks["host_zero_copy"], picks["host_zc_blocks"], record["host"] = tune_host(ctx)
     ctx.close()
     device = torch.cuda.get_device_name(0)
     date = datetime.date.today().isoformat()
     header = HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], ragged=picks["ragged_ntt_min"],
                            chunks=", ".join(str(x) for x in picks["host_chunks"]),
                            zero_copy=", ".join(str(x) for x in picks["host_zero_copy"]),
+                           zc_blocks=", ".join(str(x) for x in picks["host_zc_blocks"]),
                            add=", ".join(str(x) for x in picks["add_thread_bytes"]))
     record = {"device": device, "date": date, "torch": torch.__version__, "measured": sorted(only),
               "picks": picks, **record}

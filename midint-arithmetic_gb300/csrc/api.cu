@@ -178,8 +178,9 @@ mi_status wide_status(mi_ctx ctx) {
     return set_error(MI_ETIMEOUT, "a multi-block addition gave up waiting for a predecessor tile");
 }
 
-// Runs `launch(da, db, dr, dcarry, count, stream)` over a batch of host
-// buffers, with the tuning of operation class `cls`.  Zero-copy mode 2 with
+// Runs `launch(da, db, dr, dcarry, count, stream, max_per_sm)` over a batch of
+// host buffers, with the tuning of operation class `cls` (max_per_sm is the
+// class's zero-copy occupancy cap in mode 1, else 0).  Zero-copy mode 2 with
 // mapped pinned operands: the kernels read the operands in place and only the
 // results go through the staging slots and the copy-out stream (the two
 // directions of the host link then run at once).  Zero-copy mode 1 with
@@ -212,7 +213,7 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
         void* dc = h_carry ? mapped_host(h_carry) : nullptr;
         if (dr && (dc || !h_carry)) {
             MI_TRY(launch(const_cast<char*>(za), const_cast<char*>(zb), dr, static_cast<uint8_t*>(dc), n,
-                          ctx->pipe[2]));
+                          ctx->pipe[2], ctx->host_zc_blocks[cls]));
             MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[2]));
             return MI_OK;
         }
@@ -238,7 +239,7 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
             // writes the staging slot once its previous copy-out is done
             if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_out[slot], 0));
             MI_TRY(launch(const_cast<char*>(za) + base * in_row, const_cast<char*>(zb) + base * in_row, stg + off_r,
-                          h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt, comp));
+                          h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt, comp, 0u));
         } else {
             if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
             MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
@@ -248,7 +249,7 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
             MI_CUDA_TRY(cudaEventRecord(ctx->ev_in[slot], cin));
             MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_in[slot], 0));
             MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr,
-                          cnt, comp));
+                          cnt, comp, 0u));
         }
         MI_CUDA_TRY(cudaEventRecord(ctx->ev_k[slot], comp));
         MI_CUDA_TRY(cudaStreamWaitEvent(cout, ctx->ev_k[slot], 0));
@@ -395,6 +396,11 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             if (value > 2) return set_error(MI_EINVAL, "host zero-copy mode %u not 0, 1 or 2", value);
             ctx->host_zero_copy[cls] = value;
             return MI_OK;
+        case MI_TUNE_HOST_ZC_BLOCKS:
+            if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
+            if (value > 3) return set_error(MI_EINVAL, "zero-copy blocks per SM %u outside 0..3", value);
+            ctx->host_zc_blocks[cls] = value;
+            return MI_OK;
         case MI_TUNE_WIDE_SPIN_LIMIT:
             if (value < 1) return set_error(MI_EINVAL, "spin limit must be at least 1");
             ctx->wide.spin_limit = value;
@@ -423,8 +429,11 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
             return MI_OK;
         case MI_TUNE_HOST_CHUNKS:
         case MI_TUNE_HOST_ZERO_COPY:
+        case MI_TUNE_HOST_ZC_BLOCKS:
             if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
-            *value = knob == MI_TUNE_HOST_CHUNKS ? ctx->host_chunks[cls] : ctx->host_zero_copy[cls];
+            *value = knob == MI_TUNE_HOST_CHUNKS ? ctx->host_chunks[cls]
+                     : knob == MI_TUNE_HOST_ZERO_COPY ? ctx->host_zero_copy[cls]
+                                                     : ctx->host_zc_blocks[cls];
             return MI_OK;
         case MI_TUNE_WIDE_SPIN_LIMIT: *value = ctx->wide.spin_limit; return MI_OK;
         case MI_TUNE_WIDE_WITHHOLD: *value = ctx->wide.withhold; return MI_OK;
@@ -547,7 +556,7 @@ mi_status mi_compat_gpuAdd_u32(int num_instances, uint32_t m, const uint32_t* h_
     const size_t row = size_t(m) * 4;
     const mi_status st = host_pipeline(ctx, HOST_ADD, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [ctx, m, tb = add_bytes(ctx, m, 4)](void* da, void* db, void* dr, uint8_t*, uint32_t cnt,
-                                                              cudaStream_t st) {
+                                                              cudaStream_t st, uint32_t) {
                              return launch_add_u32(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                    static_cast<uint32_t*>(dr), nullptr, cnt, m, tb, st, &ctx->wide);
                          },
@@ -563,9 +572,9 @@ mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 8;
     return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st, uint32_t cap) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
-                                                       static_cast<uint32_t*>(dr), cnt, 2 * m, false, st);
+                                                       static_cast<uint32_t*>(dr), cnt, 2 * m, false, st, cap);
                          });
 }
 
@@ -577,9 +586,9 @@ mi_status mi_compat_gpuMultiply_u32(int num_instances, uint32_t m, const uint32_
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 4;
     return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st, uint32_t cap) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
-                                                       static_cast<uint32_t*>(dr), cnt, m, false, st);
+                                                       static_cast<uint32_t*>(dr), cnt, m, false, st, cap);
                          });
 }
 
@@ -596,7 +605,7 @@ mi_status mi_compat_gpuMulFFT_u16(int num_instances, uint32_t M, const uint16_t*
     const size_t row = size_t(m) * 8;
     // the NTT kernel, storing the low M digits (m limbs) of each product
     return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [ctx, m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                         [ctx, m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st, uint32_t) {
                              return launch_mul_ntt(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
                                                    static_cast<uint64_t*>(dr), cnt, m, ctx->ntt.params, st, true);
                          });
@@ -686,7 +695,7 @@ mi_status mi_host_add_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* h_b, 
     const size_t row = size_t(limbs) * 8;
     const mi_status st = host_pipeline(ctx, HOST_ADD, h_a, h_b, h_r, h_carry, n, row, row,
                          [ctx, limbs, tb = add_bytes(ctx, limbs, 8)](void* da, void* db, void* dr, uint8_t* dc,
-                                                                      uint32_t cnt, cudaStream_t st) {
+                                                                      uint32_t cnt, cudaStream_t st, uint32_t) {
                              return launch_add_u64(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
                                                    static_cast<uint64_t*>(dr), dc, cnt, limbs, ADD_PLAIN, tb, st,
                                                    &ctx->wide);
@@ -701,9 +710,9 @@ mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* 
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
     const size_t row = size_t(limbs) * 8;
     return host_pipeline(ctx, HOST_MUL, h_a, h_b, h_r, nullptr, n, row, 2 * row,
-                         [limbs](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st) {
+                         [limbs](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st, uint32_t cap) {
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
-                                                       static_cast<uint32_t*>(dr), cnt, 2 * limbs, true, st);
+                                                       static_cast<uint32_t*>(dr), cnt, 2 * limbs, true, st, cap);
                          });
 }
 

@@ -24,6 +24,8 @@ struct mi_ctx_s {
     // host-buffer batch, and whether kernels read mapped pinned buffers in place
     uint32_t host_chunks[2] = {mi::tuned::kHostChunks[0], mi::tuned::kHostChunks[1]};
     uint32_t host_zero_copy[2] = {mi::tuned::kHostZeroCopy[0], mi::tuned::kHostZeroCopy[1]};
+    // zero-copy mode 1: resident blocks per SM of the classical product (0: all that fit)
+    uint32_t host_zc_blocks[2] = {mi::tuned::kHostZcBlocks[0], mi::tuned::kHostZcBlocks[1]};
     std::mutex mu;  // serialises host-pointer calls on one context
     // ragged batches: products whose shorter operand has at least this many
     // u64 limbs go through the NTT kernel (at most 257: classical groups hold

@@ -38,8 +38,10 @@ uint32_t add_size_class(uint64_t bytes);
 
 // Classical multiplication on u32 limb views (a u64 buffer with m limbs is a
 // u32 buffer with 2m limbs).  full: r has 2*n32 limbs per instance, else n32.
+// max_per_sm > 0 caps the full-product kernel's resident blocks per SM (by
+// its shared-memory request).
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
-                             bool full, cudaStream_t st);
+                             bool full, cudaStream_t st, uint32_t max_per_sm = 0);
 
 // Low n32 limbs of a*b per instance (u32 limb views), n32 > 8.
 mi_status launch_mul_lo(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st);

@@ -73,40 +73,59 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 
     }
 }
 
+// Dynamic shared memory that leaves room for at most max_per_sm blocks of a
+// kernel per SM (at least `smem`, at most the per-block maximum).
+mi_status capped_smem(size_t smem, uint32_t max_per_sm, size_t* out) {
+    *out = smem;
+    if (max_per_sm == 0) return MI_OK;
+    int dev = 0, per_sm = 0, reserved = 0, per_block = 0;
+    MI_CUDA_TRY(cudaGetDevice(&dev));
+    MI_CUDA_TRY(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    MI_CUDA_TRY(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+    MI_CUDA_TRY(cudaDeviceGetAttribute(&per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    // max_per_sm + 1 blocks of `need` bytes (plus the reservation) overflow the SM
+    const size_t need = size_t(per_sm) / (max_per_sm + 1) + 1024 - size_t(reserved);
+    if (need > *out) *out = need < size_t(per_block) ? need : size_t(per_block);
+    return MI_OK;
+}
+
 template <int NT, bool VEC>
 mi_status launch_nt(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
-                    cudaStream_t st) {
+                    cudaStream_t st, uint32_t max_per_sm) {
     using S = MulShape<NT>;
     auto kern = k_mul<NT, VEC>;
-    static bool attr_done[64] = {};
+    static size_t attr_bytes[64] = {};  // the kernel's dynamic shared-memory limit, per device
     int dev = 0;
     MI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-        attr_done[dev] = true;
+    if (dev < 0 || dev >= 64) return set_error(MI_ENODEV, "device %d out of range", dev);
+    size_t smem = S::SMEM;
+    MI_TRY(capped_smem(S::SMEM, max_per_sm, &smem));
+    if (attr_bytes[dev] < smem) {
+        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        attr_bytes[dev] = smem;
     }
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
     const uint64_t cap = uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;
-    MI_CUDA_TRY(launch_pdl(kern, dim3(uint32_t(blocks)), dim3(S::BLOCK), S::SMEM, st, a, b, r, n, n32, full));
+    MI_CUDA_TRY(launch_pdl(kern, dim3(uint32_t(blocks)), dim3(S::BLOCK), smem, st, a, b, r, n, n32, full));
     return MI_OK;
 }
 
 template <bool VEC>
 mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
-                   cudaStream_t st) {
+                   cudaStream_t st, uint32_t cap) {
     const uint32_t nt = pow2ceil((n32 + T - 1) / T);
     switch (nt) {
-        case 1: return launch_nt<1, VEC>(a, b, r, n, n32, full, st);
-        case 2: return launch_nt<2, VEC>(a, b, r, n, n32, full, st);
-        case 4: return launch_nt<4, VEC>(a, b, r, n, n32, full, st);
-        case 8: return launch_nt<8, VEC>(a, b, r, n, n32, full, st);
-        case 16: return launch_nt<16, VEC>(a, b, r, n, n32, full, st);
-        case 32: return launch_nt<32, VEC>(a, b, r, n, n32, full, st);
-        case 64: return launch_nt<64, VEC>(a, b, r, n, n32, full, st);
-        case 128: return launch_nt<128, VEC>(a, b, r, n, n32, full, st);
-        case 256: return launch_nt<256, VEC>(a, b, r, n, n32, full, st);
-        case 512: return launch_nt<512, VEC>(a, b, r, n, n32, full, st);
+        case 1: return launch_nt<1, VEC>(a, b, r, n, n32, full, st, cap);
+        case 2: return launch_nt<2, VEC>(a, b, r, n, n32, full, st, cap);
+        case 4: return launch_nt<4, VEC>(a, b, r, n, n32, full, st, cap);
+        case 8: return launch_nt<8, VEC>(a, b, r, n, n32, full, st, cap);
+        case 16: return launch_nt<16, VEC>(a, b, r, n, n32, full, st, cap);
+        case 32: return launch_nt<32, VEC>(a, b, r, n, n32, full, st, cap);
+        case 64: return launch_nt<64, VEC>(a, b, r, n, n32, full, st, cap);
+        case 128: return launch_nt<128, VEC>(a, b, r, n, n32, full, st, cap);
+        case 256: return launch_nt<256, VEC>(a, b, r, n, n32, full, st, cap);
+        case 512: return launch_nt<512, VEC>(a, b, r, n, n32, full, st, cap);
         default: return set_error(MI_EINVAL, "mul: %u u32 limbs exceeds the classical maximum", n32);
     }
 }
@@ -114,11 +133,12 @@ mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n
 }  // namespace
 
 mi_status launch_mul_classic(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
-                             cudaStream_t st) {
+                             cudaStream_t st, uint32_t max_per_sm) {
     const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (n32 % 4 == 0);
     if (!full && n32 > T)  // low halves: half the partial products of a full product
         return launch_mul_lo(a, b, r, n, n32, st);
-    return vec ? dispatch<true>(a, b, r, n, n32, full, st) : dispatch<false>(a, b, r, n, n32, full, st);
+    return vec ? dispatch<true>(a, b, r, n, n32, full, st, max_per_sm)
+               : dispatch<false>(a, b, r, n, n32, full, st, max_per_sm);
 }
 
 }  // namespace mi

@@ -81,6 +81,21 @@ def test_zero_copy_on_pinned_buffers(hctx):
     assert np.array_equal(r, ra) and np.array_equal(c, ca)
 
 
+@pytest.mark.parametrize("blocks", [1, 2, 3])
+def test_zero_copy_with_capped_occupancy(hctx, blocks):
+    """Mode 1 with the product kernel held to 1..3 resident blocks per SM."""
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 1)
+    hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, blocks)
+    assert hctx.get_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1) == blocks
+    for n, m in ((1500, 128), (37, 5), (64, 512)):
+        a, b = carry_stress(n, m, seed=blocks * 100 + m)
+        pa, pb = _pinned(a), _pinned(b)
+        pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+        hctx.host_mul_full(pa, pb, pr, n, m)
+        assert np.array_equal(pr.numpy().view(np.uint64), O.mul(a, b, m, True))
+    hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, 0)
+
+
 @pytest.mark.parametrize("chunks", [1, 3, 8])
 @pytest.mark.parametrize("pinned_out", [False, True])
 def test_zero_copy_reads_with_copied_results(hctx, chunks, pinned_out):
@@ -121,5 +136,9 @@ def test_host_tuning_knobs_are_checked(hctx):
         hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 3)
     with pytest.raises(midint.MidintError):
         hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 2, 4)
+    with pytest.raises(midint.MidintError):
+        hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, 4)
+    with pytest.raises(midint.MidintError):
+        hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 2, 1)
     hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 1, 5)
     assert hctx.get_tuning(midint.TUNE_HOST_CHUNKS, 1) == 5
