@@ -347,7 +347,10 @@ def run_ours(args):
                    "l2": f"inputs rotate over {sets} operand sets of {set_bytes >> 20} MiB (> 4x L2)"},
         "roofline": {"bound": "int-mul", "achieved": achieved_prod / 1e9, "peak": peak_prod / 1e9,
                      "unit": "G 32x32-bit partial products/s", "frac": achieved_prod / peak_prod,
-                     "traffic": None,
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one k_mul<32> launch (ncu, cold, single
+                     # launch): the 32 MiB of operands read once, the product still in L2 at kernel end
+                     "traffic": 33.62e6 + 0.35e6,
+                     "traffic_source": "profiles/k_mul_16384x8192bit.md (ncu --set full, one launch)",
                      "peak_source": "measured in-process: mi_calib_mul32_peak (independent mad.lo.cc/madc.hi.cc "
                                     "chains, the kernel's own instruction mix)",
                      "per_unit": f"{prods32_per_inst} partial products per instance"},
@@ -417,7 +420,11 @@ def add_section(args, ctx, dev, stream, world, rank) -> dict:
                   "sum mod 2^4096 + carry-out byte",
         "ms_per_launch": ms, "GB/s": gbs * world, "instances/s": world * N_ADD / (ms * 1e-3),
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": (gbs / hbm) if hbm else None, "traffic": None,
+                     "frac": (gbs / hbm) if hbm else None,
+                     # one k_add launch under ncu: the two operands read once (67.12 MB), 3.98 MB of the result
+                     # written back before the kernel ended (the rest drains from L2 afterwards)
+                     "traffic": 67.12e6 + 3.98e6,
+                     "traffic_source": "profiles/k_add_65536x4096bit.md (ncu --set full, one launch)",
                      "per_unit": "1537 B per instance (2 x 512 B read, 512 B + 1 B written)",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "absent"},
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
