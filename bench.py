@@ -350,7 +350,7 @@ def run_ours(args):
                      # dram__bytes_read.sum + dram__bytes_write.sum of one k_mul<32> launch (ncu, cold, single
                      # launch): the 32 MiB of operands read once, the product still in L2 at kernel end
                      "traffic": 33.62e6 + 0.35e6,
-                     "traffic_source": "profiles/k_mul_16384x8192bit.md (ncu --set full, one launch)",
+                     "traffic_source": "ncu --set full of one k_mul<32> launch (summary committed under profiles/)",
                      "peak_source": "measured in-process: mi_calib_mul32_peak (independent mad.lo.cc/madc.hi.cc "
                                     "chains, the kernel's own instruction mix)",
                      "per_unit": f"{prods32_per_inst} partial products per instance"},
@@ -424,7 +424,7 @@ def add_section(args, ctx, dev, stream, world, rank) -> dict:
                      # one k_add launch under ncu: the two operands read once (67.12 MB), 3.98 MB of the result
                      # written back before the kernel ended (the rest drains from L2 afterwards)
                      "traffic": 67.12e6 + 3.98e6,
-                     "traffic_source": "profiles/k_add_65536x4096bit.md (ncu --set full, one launch)",
+                     "traffic_source": "ncu --set full of one k_add launch (summary committed under profiles/)",
                      "per_unit": "1537 B per instance (2 x 512 B read, 512 B + 1 B written)",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "absent"},
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
