@@ -456,5 +456,13 @@ __device__ __forceinline__ void store_block(uint32_t* rr, uint32_t o, uint32_t r
     }
 }
 
+// The same for rows that are 8-byte aligned, with o and rlen even (u64 limbs
+// seen as u32 pairs): one 8-byte store per pair of words.
+__device__ __forceinline__ void store_pairs(uint32_t* rr, uint32_t o, uint32_t rlen, const uint32_t (&v)[T]) {
+#pragma unroll
+    for (int w = 0; w < T; w += 2)
+        if (o + w < rlen) __stcs(reinterpret_cast<uint2*>(rr + o + w), make_uint2(v[w], v[w + 1]));
+}
+
 }  // namespace classic
 }  // namespace mi

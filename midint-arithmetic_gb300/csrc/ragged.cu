@@ -368,7 +368,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         chunk_add<uint32_t, T>(ulo, pend, fin, g0, p0);
         const uint32_t cin = group_carry<NT>(g0, p0, 0u, &gc, scr);
         chunk_inc<uint32_t, T>(fin, cin);
-        if (valid) classic::store_block<false>(rr, c * W + t * T, rlen, fin);
+        if (valid) classic::store_pairs(rr, c * W + t * T, rlen, fin);
         // the high half plus that carry becomes the next window (cannot overflow)
         uint32_t z[T];
 #pragma unroll
@@ -381,7 +381,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         chunk_inc<uint32_t, T>(pend, cin1);
         group_sync<NT>();  // gA and the slots are reused by the next chunk
     }
-    if (valid) classic::store_block<false>(rr, chunks * W + t * T, rlen, pend);
+    if (valid) classic::store_pairs(rr, chunks * W + t * T, rlen, pend);
 }
 
 // Comb products, shorter operand y of at most 8 limbs (16 words, held in
@@ -456,8 +456,8 @@ __device__ __forceinline__ void comb_task(const Params& P, const Task& tk) {
         chunk_add<uint32_t, K>(lo, hin, out, gg, pp);
         chunk_inc<uint32_t, K>(out, group_carry<G>(gg, pp, 0u, &gc, nullptr));
 #pragma unroll
-        for (int w = 0; w < K; ++w)
-            if (base + w < rlen) rr[base + w] = out[w];
+        for (int w = 0; w < K; w += 2)  // rows are 8-byte aligned and rlen even
+            if (base + w < rlen) *reinterpret_cast<uint2*>(rr + base + w) = make_uint2(out[w], out[w + 1]);
         // the last thread's high words plus the group's carry-out open the next pass
         uint32_t c = gc;
 #pragma unroll
@@ -470,8 +470,8 @@ __device__ __forceinline__ void comb_task(const Params& P, const Task& tk) {
     if (t == 0) {
         const uint32_t top = passes * G * K;
 #pragma unroll
-        for (int w = 0; w < NBW; ++w)
-            if (top + w < rlen) rr[top + w] = pend[w];
+        for (int w = 0; w < NBW; w += 2)
+            if (top + w < rlen) *reinterpret_cast<uint2*>(rr + top + w) = make_uint2(pend[w], pend[w + 1]);
     }
 }
 
