@@ -681,7 +681,8 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     k_scatter<<<blocks, 256, 0, st>>>(n_ops, P.scr);
     k_rg_ntt<<<persistent_grid((const void*)k_rg_ntt, kNttSmem), 256, kNttSmem, st>>>(P);
     k_rg_classic<<<persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st>>>(P);
-    k_rg_c64<<<persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st>>>(P);
+    // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
+    if (P.ntt_min > 129) k_rg_c64<<<persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st>>>(P);
     k_rg_add<<<persistent_grid((const void*)k_rg_add, 0), 256, 0, st>>>(P);
     MI_CUDA_TRY(cudaGetLastError());
     return MI_OK;
