@@ -7,11 +7,13 @@
 //
 // Here every u64 limb is one digit; the product of two m-limb integers has
 // coefficients below m * 2^128 <= 2^139 (m <= 2048), so five primes
-// p_i < 2^30 (product 2^149.4) recover every coefficient exactly by CRT.  One
-// CTA of L/8 threads owns one instance (L = pow2ceil(2m) >= 256): for each
-// prime it converts a and b into the field, runs two forward transforms,
-// multiplies pointwise and runs the inverse transform (ntt32.cuh), leaving
-// the residues in shared memory.  The same CTA then recombines each
+// p_i < 2^30 (product 2^149.4) recover every coefficient exactly by CRT; when
+// 48-bit digits fit the same transform length (2 ceil(4m/3) <= L) the kernel
+// runs them on four primes instead (ntt_mul.cuh).  One CTA of L/8 threads
+// owns one instance (L = pow2ceil(2m) >= 256): for each prime it converts a
+// and b into the field, runs two forward transforms, multiplies pointwise and
+// runs the inverse transform (ntt32.cuh), leaving the residues in shared
+// memory.  The same CTA then recombines each
 // coefficient with Garner's formula, sums the three-word coefficients of its
 // 8 output limbs, passes the overflow words to its right neighbour and
 // resolves the remaining one-bit carries with mi::group_carry -- the final
@@ -43,21 +45,21 @@ struct NttShape {
 
 // 768 threads per SM: three 256-thread CTAs for 2048-point transforms (one
 // 512-thread CTA for 4096-point ones)
-template <int LG>
+template <int LG, int NP>
 __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     k_ntt_mul(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ r, uint32_t n,
               uint32_t m, uint32_t rlen, NttMulParams P) {
     extern __shared__ __align__(16) uint32_t smem32[];
     uint32_t* scratch = smem32 + ntt32::MulSmem<LG>::WORDS32;
     for (uint64_t inst = blockIdx.x; inst < n; inst += gridDim.x)
-        ntt32::mul_one<LG>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
+        ntt32::mul_one<LG, NP == 4>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
 }
 
-template <int LG>
+template <int LG, int NP>
 mi_status launch_lg(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t m, uint32_t rlen,
                     const NttMulParams& P, cudaStream_t st) {
     using S = NttShape<LG>;
-    auto kern = k_ntt_mul<LG>;
+    auto kern = k_ntt_mul<LG, NP>;
     static bool attr_done[64] = {};
     int dev = 0;
     MI_CUDA_TRY(cudaGetDevice(&dev));
@@ -122,13 +124,18 @@ mi_status launch_mul_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
     const uint32_t rlen = low ? m : 2 * m;
     uint32_t L = pow2ceil(2 * m);
     if (L < 256) L = 256;
+    // 48-bit digits on four primes when they fit the same length
+    const bool d48 = 2 * ntt32::ntt_digits(m, true) <= L;
     const NttMulParams& P = base;
     switch (L) {
-        case 256: return launch_lg<8>(a, b, r, n, m, rlen, P, st);
-        case 512: return launch_lg<9>(a, b, r, n, m, rlen, P, st);
-        case 1024: return launch_lg<10>(a, b, r, n, m, rlen, P, st);
-        case 2048: return launch_lg<11>(a, b, r, n, m, rlen, P, st);
-        case 4096: return launch_lg<12>(a, b, r, n, m, rlen, P, st);
+        case 256: return d48 ? launch_lg<8, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<8, 5>(a, b, r, n, m, rlen, P, st);
+        case 512: return d48 ? launch_lg<9, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<9, 5>(a, b, r, n, m, rlen, P, st);
+        case 1024:
+            return d48 ? launch_lg<10, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<10, 5>(a, b, r, n, m, rlen, P, st);
+        case 2048:
+            return d48 ? launch_lg<11, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<11, 5>(a, b, r, n, m, rlen, P, st);
+        case 4096:
+            return d48 ? launch_lg<12, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<12, 5>(a, b, r, n, m, rlen, P, st);
         default: return set_error(MI_EINVAL, "ntt: %u limbs exceeds the maximum %u", m, kNttMaxLimbs);
     }
 }

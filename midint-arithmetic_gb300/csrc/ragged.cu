@@ -43,15 +43,18 @@ namespace mi {
 namespace rg {
 
 constexpr uint32_t kMaxLimbs = 1024;
-constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11
+constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11, 64-bit digits (5 primes)
+constexpr int K_N48 = 4;         // the same with 48-bit digits (4 primes)
 constexpr int K_CLS = 13;        // NT = 1..16 (one chunk), NT = 32 x chunks = 1..8
 constexpr int K_ADD = 11;        // GS = 1..32 lanes of one limb; one warp over 2..32 rows of 32 limbs
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
 constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
 constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_CMB = KEY_CLS + K_CLS, KEY_ADD = KEY_CMB + K_CMB,
-              KEY_C64 = KEY_ADD + K_ADD;
-constexpr int K = KEY_C64 + K_C64;
-constexpr int NFAM = 4;          // families: NTT, classical in a warp, additions, classical in 64 threads
+              KEY_C64 = KEY_ADD + K_ADD, KEY_N48 = KEY_C64 + K_C64;
+constexpr int K = KEY_N48 + K_N48;
+// families: NTT (64-bit digits), classical in a warp, additions, classical in
+// 64 threads, NTT with 48-bit digits
+constexpr int NFAM = 5;
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
@@ -98,9 +101,11 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
         const uint32_t s = min(la, lb), l = max(la, lb);
         if (s >= ntt_min) {
             // L must hold all la+lb output limbs (the top limb is the carry out
-            // of the last of the la+lb-1 coefficients), not only the coefficients
+            // of the last of the la+lb-1 coefficients), not only the
+            // coefficients; 48-bit digits on four primes when they fit the same L
             const uint32_t lg = max(8u, ceil_log2(la + lb));
-            return KEY_NTT + (lg - 8);
+            const uint32_t lg48 = max(8u, ceil_log2(ntt32::ntt_digits(la, true) + ntt32::ntt_digits(lb, true)));
+            return (lg48 == lg ? KEY_N48 : KEY_NTT) + (lg - 8);
         }
         if (s > 128) return KEY_C64 + (2 * l + 511) / 512 - 1;  // 64-thread groups, chunks of 256 limbs
         if (s <= 8) {  // comb: 16 words of the longer operand per thread, 512 per pass of a warp
@@ -120,7 +125,8 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
 }
 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
-    if (key < KEY_CLS) return 2048u >> (8 + key);                    // NTT: 256 threads / (L/8)
+    if (key < KEY_CLS) return 2048u >> (8 + key - KEY_NTT);          // NTT: 256 threads / (L/8)
+    if (key >= KEY_N48) return 2048u >> (8 + key - KEY_N48);
     if (key < KEY_CMB) {                                              // classical: one warp
         const uint32_t k = key - KEY_CLS;
         return k < 5 ? 32u >> k : 1u;
@@ -156,10 +162,11 @@ __global__ void __launch_bounds__(256) k_classify(const mi_op* __restrict__ ops,
 
 // First key of family f (f = NFAM: the end of the key space).
 __host__ __device__ constexpr int fam_base(int f) {
-    return f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : K)));
+    return f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : (f == 4 ? KEY_N48 : K))));
 }
 static_assert(fam_base(1) - fam_base(0) <= 32 && fam_base(2) - fam_base(1) <= 32 &&
-                  fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32,
+                  fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32 &&
+                  fam_base(5) - fam_base(4) <= 32,
               "a family's keys fit one warp");
 
 // One warp per family scans its keys in c_order (shuffle scans): op offsets
@@ -230,8 +237,8 @@ struct Task {
 };
 
 __device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
-    const int base = f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : KEY_C64));
-    const int nk = f == 0 ? K_NTT : (f == 1 ? K_CLS + K_CMB : (f == 2 ? K_ADD : K_C64));
+    const int base = fam_base(f);
+    const int nk = fam_base(f + 1) - base;
     const uint32_t* ts = scr + Scratch::TS + f + base;  // nk + 1 monotone starts
     int lo = 0, hi = nk;                                // ts[lo] <= t < ts[hi]
     while (hi - lo > 1) {
@@ -251,7 +258,7 @@ __device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
 
 // --- NTT family ----------------------------------------------------------------
 
-template <int LG>
+template <int LG, bool D48>
 __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32_t* sm, uint32_t* scr_warp) {
     constexpr int NT = (1 << LG) / 8;
     const uint32_t g = threadIdx.x / NT;
@@ -259,33 +266,39 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
     uint32_t* gsm = sm + g * ntt32::MulSmem<LG>::WORDS32;
     if (g < tk.count) {
         const mi_op op = P.ops[sorted[tk.first + g]];
-        ntt32::mul_one<LG>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb, P.ntt,
-                           gsm, scr_warp);
+        ntt32::mul_one<LG, D48>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb,
+                                P.ntt, gsm, scr_warp);
     } else {  // idle group: zero operands, no store, same barriers
-        ntt32::mul_one<LG>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
+        ntt32::mul_one<LG, D48>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
     }
 }
 
+// D48: the family of products with 48-bit digits on four primes (a kernel of
+// its own, so that neither digit mode's code raises the other's registers).
+template <bool D48>
 __global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
+    constexpr int F = D48 ? 4 : 0;  // family
     extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the 48 KiB of groups
+    uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the groups' shared memory
     __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
-    const uint32_t ntasks = P.scr[Scratch::NTASKS + 0];
-    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + F];
+    pdl_trigger();  // the next family's kernel may start as this one's blocks finish
+    if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + F, 1u);
     __syncthreads();
     for (uint32_t it = 0;; ++it) {
         const uint32_t t = s_task[it & 1];
         if (t >= ntasks) break;
-        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 0, 1u);
-        const Task tk = decode(P.scr, 0, t);
-        switch (tk.key - KEY_NTT) {
-            case 0: ntt_task<8>(P, tk, smem, scr_warp); break;
-            case 1: ntt_task<9>(P, tk, smem, scr_warp); break;
-            case 2: ntt_task<10>(P, tk, smem, scr_warp); break;
-            default: ntt_task<11>(P, tk, smem, scr_warp); break;
+        if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + F, 1u);
+        const Task tk = decode(P.scr, F, t);
+        switch (tk.key - (D48 ? KEY_N48 : KEY_NTT)) {
+            case 0: ntt_task<8, D48>(P, tk, smem, scr_warp); break;
+            case 1: ntt_task<9, D48>(P, tk, smem, scr_warp); break;
+            case 2: ntt_task<10, D48>(P, tk, smem, scr_warp); break;
+            default: ntt_task<11, D48>(P, tk, smem, scr_warp); break;
         }
         __syncthreads();  // the next index is visible; this one is read by all
     }
+    if (D48) pdl_wait();  // complete only after the task kernel launched before it
 }
 
 // --- classical family ----------------------------------------------------------
@@ -480,6 +493,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     uint32_t* wsm = smem32 + warp * CLS_WARP_WORDS;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 1];
+    pdl_trigger();
     for (;;) {
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
@@ -505,6 +519,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
         }
         __syncwarp();
     }
+    pdl_wait();  // complete only after the task kernel launched before it
 }
 
 // Products whose shorter operand has 129..256 limbs (below the NTT crossover):
@@ -514,6 +529,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_c64(Params P) {
     __shared__ uint32_t scr_warp[8];
     __shared__ uint32_t s_task[2];
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 3];
+    pdl_trigger();
     if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 3, 1u);
     __syncthreads();
     for (uint32_t it = 0;; ++it) {
@@ -523,6 +539,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_c64(Params P) {
         classic_task<64>(P, decode(P.scr, 3, t), smem32, scr_warp);
         __syncthreads();  // the next index is visible; shared memory is reused
     }
+    pdl_wait();  // complete only after the task kernel launched before it
 }
 
 // --- addition family -------------------------------------------------------------
@@ -594,6 +611,7 @@ __device__ __forceinline__ void add_rows(const Params& P, const Task& tk) {
 __global__ void __launch_bounds__(256, 4) k_rg_add(Params P) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 2];
+    pdl_trigger();
     for (;;) {
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
@@ -611,6 +629,7 @@ __global__ void __launch_bounds__(256, 4) k_rg_add(Params P) {
         }
         __syncwarp();
     }
+    pdl_wait();  // complete only after the task kernel launched before it
 }
 
 // --- host side -------------------------------------------------------------------
@@ -639,8 +658,10 @@ mi_status init_device() {
     for (int k = 0; k < K_CMB; ++k) order[KEY_CMB + k] = uint16_t(KEY_CMB + comb[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
     for (int k = 0; k < K_C64; ++k) order[KEY_C64 + k] = uint16_t(KEY_C64 + (K_C64 - 1 - k));
+    for (int k = 0; k < K_N48; ++k) order[KEY_N48 + k] = uint16_t(KEY_N48 + (K_N48 - 1 - k));
     MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
-    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_classic, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kClsSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kC64Smem)));
     g_init[dev] = true;
@@ -679,12 +700,20 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     k_classify<<<blocks, 256, 0, st>>>(ops, n_ops, P.scr, P.ntt_min);
     k_scan<<<1, 32 * NFAM, 0, st>>>(P.scr);  // the cursors were zeroed with the counts
     k_scatter<<<blocks, 256, 0, st>>>(n_ops, P.scr);
-    k_rg_ntt<<<persistent_grid((const void*)k_rg_ntt, kNttSmem), 256, kNttSmem, st>>>(P);
-    k_rg_classic<<<persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st>>>(P);
-    // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
-    if (P.ntt_min > 129) k_rg_c64<<<persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st>>>(P);
-    k_rg_add<<<persistent_grid((const void*)k_rg_add, 0), 256, 0, st>>>(P);
+    // The task kernels: the first waits for the binning like any launch; each later one is a programmatic dependent launch that does not
+    // wait at its start -- the families read the binned lists and write
+    // disjoint results, so a kernel's blocks may start on the SMs that the
+    // previous kernel's last tasks leave idle -- and waits for its predecessor
+    // only before it completes, so that the last kernel completes after all.
+    k_rg_ntt<false><<<persistent_grid((const void*)k_rg_ntt<false>, kNttSmem), 256, kNttSmem, st>>>(P);
     MI_CUDA_TRY(cudaGetLastError());
+    MI_CUDA_TRY(launch_pdl(k_rg_ntt<true>, persistent_grid((const void*)k_rg_ntt<true>, kNttSmem), 256, kNttSmem, st,
+                           P));
+    MI_CUDA_TRY(launch_pdl(k_rg_classic, persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st, P));
+    // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
+    if (P.ntt_min > 129)
+        MI_CUDA_TRY(launch_pdl(k_rg_c64, persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st, P));
+    MI_CUDA_TRY(launch_pdl(k_rg_add, persistent_grid((const void*)k_rg_add, 0), 256, 0, st, P));
     return MI_OK;
 }
 

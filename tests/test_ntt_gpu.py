@@ -75,9 +75,11 @@ def test_mul_ntt_matches_oracle(ctx, devmem, m):
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [64, 256, 1024, 2048])
+@pytest.mark.parametrize("m", [64, 96, 256, 384, 1024, 1536, 2048])
 def test_mul_ntt_maximal_coefficients(ctx, devmem, m):
-    # all-ones operands give the largest convolution coefficients (~m * 2^128)
+    # all-ones operands give the largest convolution coefficients (~m * 2^128
+    # with 64-bit digits; 96, 384 and 1536 limbs fill their transform length
+    # exactly with 48-bit digits on four primes, coefficients ~(4m/3) * 2^96)
     a = np.full(3 * m, 0xFFFFFFFFFFFFFFFF, np.uint64)
     b = a.copy()
     b[m:2 * m] = 1
