@@ -373,7 +373,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT, G, 2>(gA, gB4, slots, scr, t, ulo, uhi, valid ? (nby ? nby : 1u) : 1u);
+        classic::square_product<NT, G>(gA, gB4, slots, scr, t, ulo, uhi, valid ? (nby ? nby : 1u) : 1u);
         // limbs [cW, (c+1)W) are final: the low half plus the pending window
         uint32_t fin[T];
         bool g0, p0;
