@@ -103,7 +103,10 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
  *                            2: when the operands are mapped pinned memory,
  *                            the kernel reads them in place and the results
  *                            are copied out in chunks (the buffers must hold
- *                            the whole batch, as for the copies) */
+ *                            the whole batch, as for the copies);
+ *                            3: when the results are mapped pinned memory,
+ *                            the operands are copied in by chunks and the
+ *                            kernels write the results in place */
 enum {
     MI_TUNE_PLAIN_NTT_MIN = 0,
     MI_TUNE_RAGGED_NTT_MIN = 1,

@@ -185,7 +185,7 @@ def tune_host(ctx) -> tuple[list[int], list[int], list[int], dict]:
     for cls, name in ((0, "add"), (1, "mul")):
         cands = {}
         grid = ([(0, c, 0) for c in (2, 3, 4, 6, 8, 12, 16)] + [(1, 1, k) for k in (0, 1, 2, 3)]
-                + [(2, c, 0) for c in (2, 3, 4, 6, 8, 12)])
+                + [(2, c, 0) for c in (2, 3, 4, 6, 8, 12)] + [(3, c, 0) for c in (2, 3, 4, 6, 8, 12)])
         for zc, ch, kb in grid:
             ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
             ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)
@@ -193,12 +193,12 @@ def tune_host(ctx) -> tuple[list[int], list[int], list[int], dict]:
             cands[f"zero_copy={zc},chunks={ch},zc_blocks={kb}"] = {"zero_copy": zc, "chunks": ch, "zc_blocks": kb,
                                                                   "ms": wall(calls[cls])}
         # the pipeline's chunk count also serves callers whose buffers are
-        # not pinned, so it is the best copy pipeline's unless mode 2 (which
-        # chunks the same way) wins
+        # not pinned, so it is the best copy pipeline's unless mode 2 or 3
+        # (which chunk the same way) wins
         best_copy = min((v for v in cands.values() if v["zero_copy"] == 0), key=lambda v: v["ms"])
         best = min(cands.values(), key=lambda v: v["ms"])
         zc = best["zero_copy"]
-        ch = best["chunks"] if zc == 2 else best_copy["chunks"]
+        ch = best["chunks"] if zc in (2, 3) else best_copy["chunks"]
         kb = best["zc_blocks"] if zc == 1 else 0
         ctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, zc)
         ctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, ch)

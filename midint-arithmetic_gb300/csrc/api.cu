@@ -185,7 +185,9 @@ mi_status wide_status(mi_ctx ctx) {
 // results go through the staging slots and the copy-out stream (the two
 // directions of the host link then run at once).  Zero-copy mode 1 with
 // every buffer mapped pinned memory: one
-// launch reads and writes them in place.  Otherwise the batch is cut into
+// launch reads and writes them in place.  Mode 3 with mapped pinned results:
+// the operands go through the staging slots on the copy-in stream and the
+// kernels write the results in place (no copy-out).  Otherwise the batch is cut into
 // chunks that cycle through kSlots device staging slots: chunk c copies in on
 // the copy-in stream (after the slot's previous copy-out), computes on compute
 // stream c % 2 (always the first compute stream when `one_compute_stream`: for
@@ -203,12 +205,13 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
     // zero-copy reads of the operands (modes 1 and 2) when both are mapped
     const char* za = nullptr;
     const char* zb = nullptr;
-    if (ctx->host_zero_copy[cls]) {
+    const uint32_t mode = ctx->host_zero_copy[cls];
+    if (mode == 1 || mode == 2) {
         za = static_cast<const char*>(mapped_host(h_a));
         zb = static_cast<const char*>(mapped_host(h_b));
         if (!za || !zb) za = zb = nullptr;
     }
-    if (za && ctx->host_zero_copy[cls] == 1) {
+    if (za && mode == 1) {
         void* dr = mapped_host(h_r);
         void* dc = h_carry ? mapped_host(h_carry) : nullptr;
         if (dr && (dc || !h_carry)) {
@@ -217,6 +220,15 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
             MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[2]));
             return MI_OK;
         }
+    }
+    // mode 3: the operands are copied in by chunks and the kernels write the
+    // results in place when they (and the carries) are mapped pinned memory
+    char* zr = nullptr;
+    uint8_t* zc = nullptr;
+    if (mode == 3) {
+        zr = static_cast<char*>(mapped_host(h_r));
+        zc = h_carry ? static_cast<uint8_t*>(mapped_host(h_carry)) : nullptr;
+        if (h_carry && !zc) zr = nullptr;
     }
     const size_t per_inst = 2 * in_row + out_row + (h_carry ? 1 : 0);
     uint64_t chunk = (uint64_t(n) + ctx->host_chunks[cls] - 1) / ctx->host_chunks[cls];
@@ -241,13 +253,20 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
             MI_TRY(launch(const_cast<char*>(za) + base * in_row, const_cast<char*>(zb) + base * in_row, stg + off_r,
                           h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr, cnt, comp, 0u));
         } else {
-            if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, ctx->ev_out[slot], 0));
+            // the slot is free once its last reader is done: its copy-out,
+            // or in mode 3 the kernel itself
+            if (c >= mi_ctx_s::kSlots) MI_CUDA_TRY(cudaStreamWaitEvent(cin, zr ? ctx->ev_k[slot] : ctx->ev_out[slot], 0));
             MI_CUDA_TRY(cudaMemcpyAsync(stg, static_cast<const char*>(h_a) + base * in_row, cnt * in_row,
                                         cudaMemcpyHostToDevice, cin));
             MI_CUDA_TRY(cudaMemcpyAsync(stg + off_b, static_cast<const char*>(h_b) + base * in_row, cnt * in_row,
                                         cudaMemcpyHostToDevice, cin));
             MI_CUDA_TRY(cudaEventRecord(ctx->ev_in[slot], cin));
             MI_CUDA_TRY(cudaStreamWaitEvent(comp, ctx->ev_in[slot], 0));
+            if (zr) {
+                MI_TRY(launch(stg, stg + off_b, zr + base * out_row, zc ? zc + base : nullptr, cnt, comp, 0u));
+                MI_CUDA_TRY(cudaEventRecord(ctx->ev_k[slot], comp));
+                continue;
+            }
             MI_TRY(launch(stg, stg + off_b, stg + off_r, h_carry ? reinterpret_cast<uint8_t*>(stg + off_c) : nullptr,
                           cnt, comp, 0u));
         }
@@ -259,7 +278,12 @@ mi_status host_pipeline(mi_ctx ctx, int cls, const void* h_a, const void* h_b, v
             MI_CUDA_TRY(cudaMemcpyAsync(h_carry + base, stg + off_c, cnt, cudaMemcpyDeviceToHost, cout));
         MI_CUDA_TRY(cudaEventRecord(ctx->ev_out[slot], cout));
     }
-    MI_CUDA_TRY(cudaStreamSynchronize(cout));
+    if (zr) {
+        MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[2]));
+        MI_CUDA_TRY(cudaStreamSynchronize(ctx->pipe[3]));
+    } else {
+        MI_CUDA_TRY(cudaStreamSynchronize(cout));
+    }
     return MI_OK;
 }
 
@@ -393,7 +417,7 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             return MI_OK;
         case MI_TUNE_HOST_ZERO_COPY:
             if (cls > 1) return set_error(MI_EINVAL, "host operation class %u not 0 or 1", cls);
-            if (value > 2) return set_error(MI_EINVAL, "host zero-copy mode %u not 0, 1 or 2", value);
+            if (value > 3) return set_error(MI_EINVAL, "host zero-copy mode %u not 0, 1, 2 or 3", value);
             ctx->host_zero_copy[cls] = value;
             return MI_OK;
         case MI_TUNE_HOST_ZC_BLOCKS:

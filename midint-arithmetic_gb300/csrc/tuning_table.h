@@ -21,7 +21,7 @@ constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32,
 // large batch is cut into for copy/compute overlap, and the zero-copy mode for
 // mapped pinned buffers (0 copies, 1 kernels read and write in place, 2 kernels
 // read the operands in place and the results are copied out).
-constexpr uint32_t kHostChunks[2] = {8, 3};
+constexpr uint32_t kHostChunks[2] = {6, 3};
 constexpr uint32_t kHostZeroCopy[2] = {2, 1};
 // Zero-copy mode 1: resident blocks per SM of the classical product kernel
 // (0: as many as fit).

@@ -81,6 +81,43 @@ def test_zero_copy_on_pinned_buffers(hctx):
     assert np.array_equal(r, ra) and np.array_equal(c, ca)
 
 
+@pytest.mark.parametrize("chunks", [1, 3, 8])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_copied_operands_with_results_in_place(hctx, chunks, pinned):
+    """Mode 3: operands copied in by chunks, results written in place."""
+    for cls in (0, 1):
+        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, cls, 3)
+        hctx.set_tuning(midint.TUNE_HOST_CHUNKS, cls, chunks)
+    n, m = 515, 64
+    a, b = carry_stress(n, m, seed=chunks + 31)
+    if pinned:
+        pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+        hctx.host_mul_full(_pinned(a), _pinned(b), pr, n, m)
+        got = pr.numpy().view(np.uint64)
+    else:  # pageable results: the copy pipeline
+        got = np.zeros(2 * n * m, np.uint64)
+        hctx.host_mul_full(a, b, got, n, m)
+    assert np.array_equal(got, O.mul(a, b, m, True))
+    ra, ca = O.add(a, b, m)
+    if pinned:
+        pr = torch.zeros(n * m, dtype=torch.int64).pin_memory()
+        pc = torch.zeros(n, dtype=torch.uint8).pin_memory()
+        hctx.host_add(a, b, pr, pc, n, m)
+        r, c = pr.numpy().view(np.uint64), pc.numpy()
+    else:
+        r, c = np.zeros(n * m, np.uint64), np.zeros(n, np.uint8)
+        hctx.host_add(a, b, r, c, n, m)
+    assert np.array_equal(r, ra) and np.array_equal(c, ca)
+    # a wide addition with its results in place
+    mw = 5000
+    aw, bw = carry_stress(3, mw, seed=4)
+    rw = torch.zeros(3 * mw, dtype=torch.int64).pin_memory()
+    cw = torch.zeros(3, dtype=torch.uint8).pin_memory()
+    hctx.host_add(aw, bw, rw, cw, 3, mw)
+    raw, caw = O.add(aw, bw, mw)
+    assert np.array_equal(rw.numpy().view(np.uint64), raw) and np.array_equal(cw.numpy(), caw)
+
+
 @pytest.mark.parametrize("blocks", [1, 2, 3])
 def test_zero_copy_with_capped_occupancy(hctx, blocks):
     """Mode 1 with the product kernel held to 1..3 resident blocks per SM."""
@@ -133,7 +170,7 @@ def test_host_tuning_knobs_are_checked(hctx):
     with pytest.raises(midint.MidintError):
         hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 0, 0)
     with pytest.raises(midint.MidintError):
-        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 3)
+        hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 0, 4)
     with pytest.raises(midint.MidintError):
         hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 2, 4)
     with pytest.raises(midint.MidintError):
