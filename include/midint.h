@@ -212,9 +212,10 @@ mi_status mi_export_words(mi_ctx ctx, const uint64_t* src, uint32_t n, uint32_t 
 
 /* ---------------------------------------------------------------------------
  * Exact NTT multiplication r = a*b (n*2*limbs limbs), limbs <= 2048: every u64
- * limb is one digit, five 30-bit primes carry the convolution (Shoup and
- * Montgomery products on 32-bit residues), Garner's CRT and the final
- * carry run in the same kernel.  Replaces bmulFFT<P,M,Q>
+ * limb is one digit and five 30-bit primes carry the convolution, or, when
+ * 48-bit digits fit the same power-of-two length (2*ceil(4*limbs/3) <= L),
+ * 48-bit digits on four of the primes (Shoup and Montgomery products on
+ * 32-bit residues); Garner's CRT and the final carry run in the same kernel.  Replaces bmulFFT<P,M,Q>
  * (cuda/ker-fft-mul.cu.h:427-454) as launched by gpuMulFFT
  * (cuda/main.cu:415-520); unlike it, the result is exact at every size.
  * mi_mul_u64 picks the classical or the NTT kernel by size.
