@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(GS > 256 ? GS : 256)
 // with carry-in 0, so the kernel always completes), publishes its own
 // inclusive status, and the block redoes the carry pass with that carry-in.
 // The walk back is done by a warp, 32 predecessors per step.
-// Status word: bits 0-1 state (1 aggregate, 2 inclusive), bit 2 carry value.
+// Status word: bits 0-1 state (1 aggregate, 2 inclusive), bit 2 carry value,
+// bits 3-31 the launch's epoch (a word of another epoch is unpublished).
 
 constexpr uint32_t ST_AGG = 1u, ST_INC = 2u;
 
@@ -237,15 +238,19 @@ template <typename L, bool VEC, int OP>
 __global__ void __launch_bounds__(256)
     k_add_wide(const L* __restrict__ a, const L* __restrict__ b, L* __restrict__ r, uint8_t* __restrict__ carry,
                uint32_t m, uint32_t tiles_per, uint32_t n_tiles, uint32_t* status, uint32_t spin_limit,
-               uint32_t withhold) {
+               uint32_t withhold, uint64_t base, uint32_t epoch) {
     constexpr int Q = 64 / int(sizeof(L));
     constexpr uint32_t W = 256u * Q;  // limbs per tile
     __shared__ uint32_t scratch[8];
     __shared__ uint64_t shift[8];
     __shared__ uint32_t s_tile, s_cin;
-    uint32_t* counter = status + kWideTiles;
-    uint32_t* err = status + kWideTiles + 1;
-    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+    // a monotonic tile counter (this launch's tiles are base .. base+n_tiles-1)
+    // and tile words tagged with the launch's epoch: nothing is cleared
+    // between launches; a word of an older epoch reads as unpublished
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(status + kWideTiles);
+    uint32_t* err = status + kWideTiles + 2;
+    pdl_wait();  // launched with launch_pdl: the previous launch has completed
+    if (threadIdx.x == 0) s_tile = uint32_t(atomicAdd(counter, 1ull) - base);
     __syncthreads();
     const uint32_t tile = s_tile;
     if (tile >= n_tiles) return;  // (the grid has exactly n_tiles blocks)
@@ -306,13 +311,14 @@ __global__ void __launch_bounds__(256)
         // every tile between (all propagating aggregates) has published
         uint32_t cin = local_cin;
         if (!local_ok) {
-            if (t == 0) st_release(status + tile, P ? ST_AGG : (ST_INC | (gc0 << 2)));
+            if (t == 0) st_release(status + tile, (epoch << 3) | (P ? ST_AGG : (ST_INC | (gc0 << 2))));
             const int32_t first = int32_t(tile - j);  // the instance's first tile: always inclusive
             int32_t k = int32_t(tile) - 1;
             uint32_t spins = 0;
             for (;;) {
                 const int32_t i = k - int32_t(t);
-                const uint32_t sv = i >= first ? ld_acquire(status + i) : ST_INC;
+                const uint32_t raw = i >= first ? ld_acquire(status + i) : ((epoch << 3) | ST_INC);
+                const uint32_t sv = (raw >> 3) == epoch ? (raw & 7u) : 0u;
                 const uint32_t inc = __ballot_sync(MI_FULL_MASK, (sv & 3u) == ST_INC);
                 const uint32_t pending = __ballot_sync(MI_FULL_MASK, (sv & 3u) == 0u);
                 const uint32_t nearest = inc ? uint32_t(__ffs(inc) - 1) : 32u;
@@ -333,7 +339,8 @@ __global__ void __launch_bounds__(256)
             }
         }
         if (t == 0) {
-            if (!(withhold && j == 0)) st_release(status + tile, ST_INC | ((gc0 | (P ? cin : 0u)) << 2));
+            if (!(withhold && j == 0))
+                st_release(status + tile, (epoch << 3) | ST_INC | ((gc0 | (P ? cin : 0u)) << 2));
             s_cin = cin;
         }
     }
@@ -355,10 +362,12 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Rounds of whole instances, at most kWideTiles tiles each; every round
-// clears its tile words and the counter first.
+// Rounds of whole instances, at most kWideTiles tiles each; every round is a
+// new epoch of the tile words and takes the next n_tiles values of the tile
+// counter, so nothing is cleared between launches (the words are cleared
+// only when the 29-bit epoch wraps).
 template <typename L, bool VEC, int OP>
-mi_status launch_wide(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, const WideState& w,
+mi_status launch_wide(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, uint32_t m, WideState& w,
                       cudaStream_t st) {
     constexpr uint32_t W = 256u * (64 / uint32_t(sizeof(L)));
     const uint32_t tiles_per = (m + W - 1) / W;
@@ -368,12 +377,16 @@ mi_status launch_wide(const L* a, const L* b, L* r, uint8_t* carry, uint32_t n, 
     for (uint32_t i0 = 0; i0 < n; i0 += per_round) {
         const uint32_t k = (n - i0) < per_round ? (n - i0) : per_round;
         const uint32_t n_tiles = k * tiles_per;
-        MI_CUDA_TRY(cudaMemsetAsync(w.status, 0, size_t(n_tiles) * 4, st));
-        MI_CUDA_TRY(cudaMemsetAsync(w.status + kWideTiles, 0, 4, st));
+        if (w.epoch >= (1u << 29) - 1) {  // the epoch field wraps: start over from cleared words
+            MI_CUDA_TRY(cudaMemsetAsync(w.status, 0, size_t(kWideTiles) * 4, st));
+            w.epoch = 0;
+        }
+        ++w.epoch;
         const uint64_t o = uint64_t(i0) * m;
-        k_add_wide<L, VEC, OP><<<n_tiles, 256, 0, st>>>(a + o, b + o, r + o, carry ? carry + i0 : nullptr, m,
-                                                        tiles_per, n_tiles, w.status, w.spin_limit, w.withhold);
-        MI_CUDA_TRY(cudaGetLastError());
+        MI_CUDA_TRY(launch_pdl(k_add_wide<L, VEC, OP>, dim3(n_tiles), dim3(256), 0, st, a + o, b + o, r + o,
+                               carry ? carry + i0 : nullptr, m, tiles_per, n_tiles, w.status, w.spin_limit,
+                               w.withhold, w.issued, w.epoch));
+        w.issued += n_tiles;  // every block of the launch takes one counter value
     }
     return MI_OK;
 }
@@ -434,7 +447,7 @@ uint32_t add_size_class(uint64_t bytes) {
 }
 
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st, const WideState* wide) {
+                         uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st, WideState* wide) {
     const bool vec = aligned16(a) && aligned16(b) && aligned16(r) && (limbs % 2 == 0);
     if (limbs > kAddMaxLimbs64) {
         if (wide == nullptr || wide->status == nullptr) return set_error(MI_EINVAL, "add: no multi-block state");
@@ -453,7 +466,7 @@ mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
 }
 
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, const WideState* wide) {
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, WideState* wide) {
     // An even number of u32 limbs on 8-byte aligned rows is the same bytes as
     // half as many u64 limbs, with the same carry-out.
     if (limbs % 2 == 0 && aligned8(a) && aligned8(b) && aligned8(r))

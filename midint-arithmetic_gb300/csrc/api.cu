@@ -172,9 +172,9 @@ void* mapped_host(const void* p) {
 // context gave up a bounded wait; call after its stream has been synchronised.
 mi_status wide_status(mi_ctx ctx) {
     uint32_t err = 0;
-    MI_CUDA_TRY(cudaMemcpy(&err, ctx->wide.status + kWideTiles + 1, 4, cudaMemcpyDeviceToHost));
+    MI_CUDA_TRY(cudaMemcpy(&err, ctx->wide.status + kWideTiles + 2, 4, cudaMemcpyDeviceToHost));
     if (err == 0) return MI_OK;
-    MI_CUDA_TRY(cudaMemset(ctx->wide.status + kWideTiles + 1, 0, 4));
+    MI_CUDA_TRY(cudaMemset(ctx->wide.status + kWideTiles + 2, 0, 4));
     return set_error(MI_ETIMEOUT, "a multi-block addition gave up waiting for a predecessor tile");
 }
 
@@ -332,7 +332,7 @@ mi_status mi_ctx_create(int device, mi_ctx* out) {
             st = set_error(MI_ECUDA, "mi_ctx_create: event creation failed");
     if (st == MI_OK) st = ntt_tables_create(&ctx->ntt);
     if (st == MI_OK) {
-        const size_t wb = (size_t(kWideTiles) + 2) * 4;
+        const size_t wb = (size_t(kWideTiles) + 4) * 4;
         if (cudaMalloc(&ctx->wide.status, wb) != cudaSuccess || cudaMemset(ctx->wide.status, 0, wb) != cudaSuccess)
             st = set_error(MI_ENOMEM, "mi_ctx_create: multi-block addition state");
     }

@@ -13,12 +13,15 @@ enum AddOp : int { ADD_PLAIN = 0, ADD_SIX = 1 };
 // Batched addition on u64 or u32 limbs (op = ADD_PLAIN or ADD_SIX).
 // Arguments are already validated; n > 0, limbs > 0.
 // Device state of the additions wider than one block (decoupled look-back):
-// `status` holds kWideTiles tile words, then the tile counter, then the error
-// word (set when a bounded wait gave up).  One per context; wide additions on
-// one context must not overlap on the device.
+// `status` holds kWideTiles tile words, then the 64-bit tile counter, then the
+// error word (set when a bounded wait gave up).  One per context; wide
+// additions on one context must not overlap on the device.  The host side
+// keeps the epoch of the last launch and the counter values issued so far.
 constexpr uint32_t kWideTiles = 1u << 16;
 struct WideState {
-    uint32_t* status = nullptr;    // kWideTiles + 2 words
+    uint32_t* status = nullptr;    // kWideTiles + 4 words
+    uint32_t epoch = 0;            // of the last launch (tile words carry it)
+    uint64_t issued = 0;           // tile counter values taken by earlier launches
     uint32_t spin_limit = 1u << 20;  // polls of an unpublished predecessor before giving up
     uint32_t withhold = 0;         // tests only: first tiles never publish (makes the waits run out)
     uint32_t round_tiles = kWideTiles;  // tiles per launch (at most kWideTiles)
@@ -30,9 +33,9 @@ struct WideState {
 // kernel, which needs `wide`.
 mi_status launch_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* carry, uint32_t n,
                          uint32_t limbs, int op, uint32_t thread_bytes, cudaStream_t st,
-                         const WideState* wide = nullptr);
+                         WideState* wide = nullptr);
 mi_status launch_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* carry, uint32_t n,
-                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, const WideState* wide = nullptr);
+                         uint32_t limbs, uint32_t thread_bytes, cudaStream_t st, WideState* wide = nullptr);
 // Size class of an addition of `bytes` per operand: ceil(log2(u64 limbs)).
 uint32_t add_size_class(uint64_t bytes);
 
