@@ -6,14 +6,17 @@
 // Stages, all asynchronous on one stream (and so capturable in a CUDA graph):
 //  1. classify: each op gets a size-class key; blocks count their keys in
 //     shared memory and add the counts to the global ones;
-//  2. scan (one thread per family): op offsets per key and task offsets per
+//  2. scan (one warp per family): op offsets per key and task offsets per
 //     family, with the keys of each family in descending cost order;
 //  3. scatter: op indices grouped by key (each block reserves its slots of a
 //     key with one atomic);
-//  4. four persistent kernels, one per family, each popping tasks from its
-//     atomic queue:
+//  4. one persistent kernel per family, each popping tasks from its atomic
+//     queue, chained so that each kernel's blocks start on the SMs the
+//     previous kernel's last tasks leave idle (ragged_launch):
 //     * NTT products (shorter operand >= the crossover): a task is one CTA of
-//       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh);
+//       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh),
+//       one family with 64-bit digits on five primes and one with 48-bit
+//       digits on four for the products whose 48-bit digits fit the same L;
 //     * classical products with a shorter operand of up to 128 limbs, a task
 //       per warp: comb products when it has at most 8 limbs (each thread
 //       multiplies 16 words of the longer operand by all of it in registers),
