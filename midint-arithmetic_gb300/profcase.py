@@ -8,7 +8,8 @@ when --warmup 1) with seeded inputs already resident on the device:
   mul     16384 x 128 u64 limbs, full products  (k_mul)
   mul_lo  the same batch, low halves            (k_mul_lo)
   poly    the same batch                        (k_poly)
-  ntt     1024 x 1024 u64 limbs                 (k_ntt_mul)
+  ntt     1024 x 1024 u64 limbs                 (k_ntt_mul, 64-bit digits on five primes)
+  ntt48   1024 x 768 u64 limbs                  (k_ntt_mul, 48-bit digits on four primes, L = 2048)
   ragged  a mixed ragged list (--ragged-ops)    (k_classify, k_scan, k_scatter, k_rg_*)
   wide    16 pairs x 2^21 u64 limbs             (k_add_wide)
   convert the addition batch to big-endian 8-byte words and back (k_export, k_count_words, k_import)
@@ -85,6 +86,11 @@ def main():
         na, nb = dput(a), dput(b)
         nr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
         calls.append(lambda: ctx.mul_ntt(na, nb, nr, 1024, 1024, stream=sp))
+    if "ntt48" in ops:
+        a4, b4 = workloads.ntt_pairs(n=1024, m=768)
+        qa, qb = dput(a4), dput(b4)
+        qr = torch.empty(2 * a4.size, dtype=torch.int64, device=dev)
+        calls.append(lambda: ctx.mul_ntt(qa, qb, qr, 1024, 768, stream=sp))
     if "wide" in ops:
         wa, wb = workloads.add_pairs(n=16, m=1 << 21, worst_every=8)
         xa, xb = dput(wa), dput(wb)
