@@ -16,6 +16,10 @@ when --warmup 1) with seeded inputs already resident on the device:
   ragged_bands  the --ragged-ops list cut into its additions and its products
           by shorter-operand band, each band timed alone as its own captured
           ragged run (CUDA events over 10 replays after 3) and printed as JSON
+  ntt_sizes  NTT products at 384/400, 768/800 and 1536/1600 limbs (the first of
+          each pair takes 48-bit digits on four primes, the second 64-bit
+          digits on five, at the same transform length), ns per product with
+          CUDA events over 10 launches after 3, printed as JSON
   wide_variants  additions of 16 pairs x 2^21 u64 limbs with no all-ones pair,
           every 8th pair all-ones + 1, and every pair all-ones + 1 (the
           carry runs through every tile), each timed with CUDA events over
@@ -118,8 +122,37 @@ def main():
         print(json.dumps(ragged_bands(ctx, dev, sp, args.ragged_ops), indent=1))
     if "wide_variants" in ops:
         print(json.dumps(wide_variants(ctx, dev, sp), indent=1))
+    if "ntt_sizes" in ops:
+        print(json.dumps(ntt_sizes(ctx, dev, sp), indent=1))
     ctx.close()
     print("profcase: ran", ",".join(ops))
+
+
+def ntt_sizes(ctx, dev, sp) -> dict:
+    """ns per NTT product at sizes either side of the 48-bit digit limit."""
+    import torch
+
+    import workloads
+
+    res = {}
+    for m in (384, 400, 768, 800, 1536, 1600):
+        n = 2048 * 1024 // m  # about 2^21 limbs per operand array
+        a, b = workloads.ntt_pairs(n=n, m=m)
+        da = torch.from_numpy(a.view(np.int64)).to(dev)
+        db = torch.from_numpy(b.view(np.int64)).to(dev)
+        dr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        for _ in range(3):
+            ctx.mul_ntt(da, db, dr, n, m, stream=sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ctx.mul_ntt(da, db, dr, n, m, stream=sp)
+        e1.record()
+        e1.synchronize()
+        res[str(m)] = {"instances": n, "ns_per_product": e0.elapsed_time(e1) / 10 * 1e6 / n}
+        del da, db, dr
+        torch.cuda.empty_cache()
+    return res
 
 
 def wide_variants(ctx, dev, sp) -> dict:
