@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
     ap.add_argument("--ragged-ops", type=int, default=200000, help="ops in the ragged batch")
     ap.add_argument("--sections", default="add,ntt,ragged,serving,u32,fused,wide",
-                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused, wide)")
+                    help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused, wide; "
+                         "sweep, the reference driver's size sweep, runs only when named)")
     return ap.parse_args()
 
 
@@ -388,7 +389,61 @@ def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
         res["fused"] = fused_section(args, ctx, dev, stream, world, rank)
     if "wide" in sections:
         res["wide_add"] = wide_section(args, ctx, dev, stream, world, rank)
+    if "sweep" in sections:  # opt-in: not among the defaults
+        res["size_sweep"] = size_sweep(args, ctx, dev, stream, world, rank)
     return res
+
+
+def ref_u32_ops(m32: int) -> float:
+    """The reference driver's normalised operation count of one product of
+    m32-word operands, 300 m lg m (numAd32OpsOfMultInst, cuda/helper.h:37-43),
+    which its Gu32ops/s figures divide by the time."""
+    return 300.0 * m32 * (m32.bit_length() - 1)
+
+
+def size_sweep(args, ctx, dev, stream, world, rank) -> dict:
+    """Every size the reference driver sweeps (cuda/main.cu:661-746): operands
+    of 16..4096 u32 words (512..131072 bits) with 2^24 words per operand array
+    (the instance count shrinks as the size grows); addition in GB/s (3 words
+    moved per operand word, the driver's count), the low-half classical
+    product (the driver's gpuMultiply semantics) and the NTT product in
+    products/s and in the driver's normalised Gu32ops/s.  Two operand sets
+    rotate (256 MiB > L2)."""
+    import torch
+
+    import workloads
+
+    sp = stream.cuda_stream
+    hbm = measured_peaks().get("hbm_gbs")
+    total = 1 << 24  # u32 words per operand array
+    out = {"config": "operands of 16..4096 u32 words, 2^24 words per operand array, 2 rotating sets",
+           "sizes": {}}
+    for m32 in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096):
+        m = m32 // 2  # u64 limbs
+        n = total // m32
+        a, b = workloads.mul_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 9, rank) + m32)
+        with torch.cuda.stream(stream):
+            da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(2)]
+            db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(2)]
+            dr = [torch.empty(2 * a.size, dtype=torch.int64, device=dev) for _ in range(2)]
+        torch.cuda.synchronize()
+        row = {"instances": n}
+        ms = max_over_ranks(world, time_device(lambda i: ctx.add(da[i], db[i], dr[i], n, m, stream=sp), 2, 20, 3,
+                                               stream))
+        gbs = 3.0 * n * m * 8 / (ms * 1e-3) / 1e9
+        row["add"] = {"ms": ms, "GB/s": world * gbs, "frac_hbm": (gbs / hbm) if hbm else None}
+        ms = max_over_ranks(world, time_device(lambda i: ctx.mul_lo(da[i], db[i], dr[i], n, m, stream=sp), 2, 10, 3,
+                                               stream))
+        row["mul_lo"] = {"ms": ms, "products/s": world * n / (ms * 1e-3),
+                         "Gu32ops/s": world * n * ref_u32_ops(m32) / (ms * 1e-3) / 1e9}
+        ms = max_over_ranks(world, time_device(lambda i: ctx.mul_ntt(da[i], db[i], dr[i], n, m, stream=sp), 2, 10, 3,
+                                               stream))
+        row["mul_ntt"] = {"ms": ms, "products/s": world * n / (ms * 1e-3),
+                          "Gu32ops/s": world * n * ref_u32_ops(m32) / (ms * 1e-3) / 1e9}
+        out["sizes"][str(m32 * 32)] = row
+        del da, db, dr
+        torch.cuda.empty_cache()
+    return out
 
 
 def add_section(args, ctx, dev, stream, world, rank) -> dict:
