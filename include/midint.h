@@ -83,14 +83,19 @@ mi_stream mi_ctx_stream(mi_ctx ctx);
  * product through the NTT kernel when its shorter operand has at least
  * ragged_ntt_min limbs (1..257; classical groups hold at most 256), and
  * mi_mul_u64 does so when its operands have at least plain_ntt_min limbs
- * (1..1025; 1025 = never).  Defaults come from the committed tuning table. */
+ * (1..2049; 2049 = never).  Defaults come from the committed tuning table.
+ * (mi_mul_lo_u64 has its own crossover, MI_TUNE_LO_NTT_MIN.) */
 mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t plain_ntt_min);
 
 /* Tunable launch choices of a context.  A new context starts from the table
  * that the project's autotuner measured and committed; these calls override
  * one entry (the autotuner itself sweeps candidates through them).
- *   MI_TUNE_PLAIN_NTT_MIN    cls ignored; value 1..1025 (as plain_ntt_min)
+ *   MI_TUNE_PLAIN_NTT_MIN    cls ignored; value 1..2049 (as plain_ntt_min)
  *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..257 (as ragged_ntt_min)
+ *   MI_TUNE_LO_NTT_MIN       cls ignored; value 1..2049: mi_mul_lo_u64 and
+ *                            the u64 gpuMultiply wrapper compute the low
+ *                            half with the NTT kernel from this many limbs
+ *                            on (2049 = never)
  *   MI_TUNE_ADD_THREAD_BYTES cls = ceil(log2(u64 limbs)) 0..12 of the
  *                            operands; value = bytes of each operand one
  *                            thread owns: 16, 32 or 64
@@ -123,12 +128,13 @@ enum {
     MI_TUNE_WIDE_ROUND_TILES = 7, /* cls ignored; 1..65536: tiles (2048 u64 limbs
                                    * each) per multi-block launch; an instance
                                    * may not need more (default 65536) */
-    MI_TUNE_HOST_ZC_BLOCKS = 8    /* cls as for MI_TUNE_HOST_CHUNKS; value 0..3:
+    MI_TUNE_HOST_ZC_BLOCKS = 8,   /* cls as for MI_TUNE_HOST_CHUNKS; value 0..3:
                                    * with zero-copy mode 1, at most this many
                                    * blocks per SM for the classical
                                    * multiplication kernel (0: as many as fit).
                                    * Fewer resident blocks make the first
                                    * results leave over the host link sooner */
+    MI_TUNE_LO_NTT_MIN = 9
 };
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
 
@@ -167,6 +173,10 @@ mi_status mi_add6_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t
  * mi_mul_lo_*:   r = a*b mod 2^(bits*limbs)   (n*limbs limbs)  -- the
  *                reference's bmulKerQ semantics (cuda/ker-classic-mul.cu.h:
  *                468-498, driven by gpuMultiply cuda/main.cu:221-315).
+ *                mi_mul_lo_u64 switches to the exact NTT kernel, storing the
+ *                low limbs only, from MI_TUNE_LO_NTT_MIN limbs on (tuned:
+ *                where the NTT's full product costs less than the classical
+ *                low half); the result is the same either way.
  * mi_mul_full_*: r = a*b                      (n*2*limbs limbs).
  * r must not overlap a or b.
  * ------------------------------------------------------------------------- */

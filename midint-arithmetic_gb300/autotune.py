@@ -13,6 +13,7 @@ Knobs:
   * plain classical/NTT crossover of mi_mul_u64: both paths timed on square
     products from 64 to 1024 u64 limbs; the crossover is the smallest measured
     size from which the NTT is faster at every larger measured size;
+  * the same for the low half (mi_mul_lo_u64), 256 to 2048 limbs;
   * ragged classical/NTT crossover: the 200000-op mixed ragged workload (40%
     adds, operand bits log-uniform in [256, 65536]) timed end to end for every
     candidate threshold; the fastest wins;
@@ -112,11 +113,45 @@ def tune_plain_crossover(ctx, stream, dev) -> tuple[int, dict]:
         ntt_faster[m] = t_ntt < t_cls
         del a, b, r
         torch.cuda.empty_cache()
-    pick = 1025
+    pick = 2049
     for i, m in enumerate(sizes):
         if all(ntt_faster[x] for x in sizes[i:]):
             pick = m
             break
+    return pick, record
+
+
+def tune_lo_crossover(ctx, stream, dev) -> tuple[int, dict]:
+    """Low-half products, classical (the knob at 2049) against the NTT (the
+    knob at 1) through mi_mul_lo_u64, from 256 to 2048 u64 limbs, picked as
+    for the plain crossover."""
+    import torch
+
+    import midint
+
+    sizes = [256, 320, 384, 448, 512, 640, 768, 1024, 1536, 2048]
+    record, ntt_faster = {}, {}
+    sp = stream.cuda_stream
+    for m in sizes:
+        n = max(256, (64 << 20) // (8 * m))
+        a = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        b = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        r = torch.empty(n * m, dtype=torch.int64, device=dev)
+        t = {}
+        for name, knob in (("classical", 2049), ("ntt", 1)):
+            ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, knob)
+            t[name] = _timer(lambda: ctx.mul_lo(a, b, r, n, m, stream=sp), 5, 2, stream)
+        record[str(m)] = {"instances": n, "classical_ns_per_product": t["classical"] * 1e6 / n,
+                          "ntt_ns_per_product": t["ntt"] * 1e6 / n}
+        ntt_faster[m] = t["ntt"] < t["classical"]
+        del a, b, r
+        torch.cuda.empty_cache()
+    pick = 2049
+    for i, m in enumerate(sizes):
+        if all(ntt_faster[x] for x in sizes[i:]):
+            pick = m
+            break
+    ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, pick)
     return pick, record
 
 
@@ -223,6 +258,9 @@ namespace tuned {{
 
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
 constexpr uint32_t kPlainNttMin = {plain};
+// mi_mul_lo_u64: low halves of products of at least this many u64 limbs come
+// from the NTT kernel (2049 = never).
+constexpr uint32_t kLoNttMin = {lo};
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = {ragged};
@@ -249,7 +287,7 @@ def main():
     ap.add_argument("--out-dir", default=".")
     ap.add_argument("--apply", action="store_true", help="write into the package (csrc/, tuning.json)")
     ap.add_argument("--ragged-ops", type=int, default=200000)
-    ap.add_argument("--only", default="add,plain,ragged,host", help="knob groups to measure (others keep the table)")
+    ap.add_argument("--only", default="add,plain,lo,ragged,host", help="knob groups to measure (others keep the table)")
     args = ap.parse_args()
 
     import torch
@@ -267,11 +305,14 @@ def main():
     picks.setdefault("host_chunks", [4, 6])
     picks.setdefault("host_zero_copy", [0, 1])
     picks.setdefault("host_zc_blocks", [0, 0])
-    record = {k: old.get(k) for k in ("add", "plain_crossover", "ragged_crossover", "host")}
+    picks.setdefault("lo_ntt_min", 2049)
+    record = {k: old.get(k) for k in ("add", "plain_crossover", "lo_crossover", "ragged_crossover", "host")}
     if "add" in only:
         picks["add_thread_bytes"], record["add"] = tune_add(ctx, stream, dev)
     if "plain" in only:
         picks["plain_ntt_min"], record["plain_crossover"] = tune_plain_crossover(ctx, stream, dev)
+    if "lo" in only:
+        picks["lo_ntt_min"], record["lo_crossover"] = tune_lo_crossover(ctx, stream, dev)
     if "ragged" in only:
         picks["ragged_ntt_min"], record["ragged_crossover"] = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
     if "host" in only:
@@ -279,7 +320,8 @@ def main():
     ctx.close()
     device = torch.cuda.get_device_name(0)
     date = datetime.date.today().isoformat()
-    header = HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], ragged=picks["ragged_ntt_min"],
+    header = HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], lo=picks["lo_ntt_min"],
+                           ragged=picks["ragged_ntt_min"],
                            chunks=", ".join(str(x) for x in picks["host_chunks"]),
                            zero_copy=", ".join(str(x) for x in picks["host_zero_copy"]),
                            zc_blocks=", ".join(str(x) for x in picks["host_zc_blocks"]),

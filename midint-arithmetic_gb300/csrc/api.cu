@@ -103,8 +103,11 @@ mi_status add_any(mi_ctx ctx, const void* a, const void* b, void* r, uint8_t* ca
                           static_cast<uint32_t*>(r), carry, n, limbs, tb, st, &ctx->wide);
 }
 
+// pick_ntt: a low half of at least ctx->lo_ntt_min u64 limbs comes from the
+// NTT kernel (same result; the NTT's cost grows as L lg L, the classical low
+// half's as limbs^2)
 mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n, uint32_t limbs, mi_stream stream,
-                  int limb_bytes, bool full) {
+                  int limb_bytes, bool full, bool pick_ntt = false) {
     const uint32_t maxl = kMulMaxN32 / (limb_bytes / 4);
     MI_TRY(check_batch(a, b, r, limbs, maxl, full ? "mul_full" : "mul_lo"));
     const size_t in_bytes = size_t(n) * limbs * limb_bytes;
@@ -113,6 +116,9 @@ mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n,
         return set_error(MI_EINVAL, "mul: result overlaps an operand");
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
+    if (pick_ntt && !full && limb_bytes == 8 && limbs >= ctx->lo_ntt_min && limbs <= kNttMaxLimbs)
+        return launch_mul_ntt(static_cast<const uint64_t*>(a), static_cast<const uint64_t*>(b),
+                              static_cast<uint64_t*>(r), n, limbs, ctx->ntt.params, pick_stream(ctx, stream), true);
     const uint32_t n32 = limbs * uint32_t(limb_bytes / 4);
     return launch_mul_classic(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b),
                               static_cast<uint32_t*>(r), n, n32, full, pick_stream(ctx, stream));
@@ -404,6 +410,11 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             if (value < 1 || value > 257) return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..257", value);
             ctx->ragged_ntt_min = value;
             return MI_OK;
+        case MI_TUNE_LO_NTT_MIN:
+            if (value < 1 || value > kNttMaxLimbs + 1)
+                return set_error(MI_EINVAL, "lo_ntt_min %u outside 1..%u", value, kNttMaxLimbs + 1);
+            ctx->lo_ntt_min = value;
+            return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:
             if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
             if (value != 16 && value != 32 && value != 64)
@@ -447,6 +458,7 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
     switch (knob) {
         case MI_TUNE_PLAIN_NTT_MIN: *value = ctx->plain_ntt_min; return MI_OK;
         case MI_TUNE_RAGGED_NTT_MIN: *value = ctx->ragged_ntt_min; return MI_OK;
+        case MI_TUNE_LO_NTT_MIN: *value = ctx->lo_ntt_min; return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:
             if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
             *value = ctx->add_thread_bytes[cls];
@@ -483,7 +495,7 @@ mi_status mi_add6_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t
 
 mi_status mi_mul_lo_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                         mi_stream stream) {
-    return mul_any(ctx, a, b, r, n, limbs, stream, 8, false);
+    return mul_any(ctx, a, b, r, n, limbs, stream, 8, false, true);
 }
 mi_status mi_mul_lo_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t limbs,
                         mi_stream stream) {
@@ -595,8 +607,13 @@ mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 8;
+    const bool ntt = m >= ctx->lo_ntt_min && m <= kNttMaxLimbs;  // as mi_mul_lo_u64 picks
     return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
-                         [m](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st, uint32_t cap) {
+                         [ctx, m, ntt](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st,
+                                       uint32_t cap) {
+                             if (ntt)
+                                 return launch_mul_ntt(static_cast<uint64_t*>(da), static_cast<uint64_t*>(db),
+                                                       static_cast<uint64_t*>(dr), cnt, m, ctx->ntt.params, st, true);
                              return launch_mul_classic(static_cast<uint32_t*>(da), static_cast<uint32_t*>(db),
                                                        static_cast<uint32_t*>(dr), cnt, 2 * m, false, st, cap);
                          });

@@ -33,6 +33,9 @@ struct mi_ctx_s {
     uint32_t ragged_ntt_min = mi::tuned::kRaggedNttMin;
     // mi_mul_u64: square products of at least this many u64 limbs use the NTT
     uint32_t plain_ntt_min = mi::tuned::kPlainNttMin;
+    // mi_mul_lo_u64 and the u64 gpuMultiply wrapper: low halves of products
+    // of at least this many u64 limbs come from the NTT kernel
+    uint32_t lo_ntt_min = mi::tuned::kLoNttMin;
     // multi-block additions: tile status words, counter and error word
     mi::WideState wide;
     // addition: operand bytes per thread by size class ceil(log2(u64 limbs))

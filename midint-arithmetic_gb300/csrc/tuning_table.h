@@ -11,6 +11,9 @@ namespace tuned {
 
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
 constexpr uint32_t kPlainNttMin = 160;
+// mi_mul_lo_u64: low halves of products of at least this many u64 limbs come
+// from the NTT kernel (2049 = never).
+constexpr uint32_t kLoNttMin = 320;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = 96;

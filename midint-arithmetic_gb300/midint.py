@@ -34,7 +34,7 @@ RAGGED_NOALLOC_MAX_OPS = 65536
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
 _S = ctypes.c_int  # mi_status
 (TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES, TUNE_HOST_CHUNKS, TUNE_HOST_ZERO_COPY,
- TUNE_WIDE_SPIN_LIMIT, TUNE_WIDE_WITHHOLD, TUNE_WIDE_ROUND_TILES, TUNE_HOST_ZC_BLOCKS) = range(9)
+ TUNE_WIDE_SPIN_LIMIT, TUNE_WIDE_WITHHOLD, TUNE_WIDE_ROUND_TILES, TUNE_HOST_ZC_BLOCKS, TUNE_LO_NTT_MIN) = range(10)
 SIGNATURES = {
     "mi_version": (_I, []),
     "mi_status_string": (ctypes.c_char_p, [_I]),

@@ -90,9 +90,36 @@ def test_mul_config_shape(ctx, devmem):
     assert np.array_equal(got32.view(np.uint64), got[: 64 * 256])
 
 
+@pytest.mark.parametrize("m", [255, 256, 300, 384, 447, 448, 500, 512, 1000, 1024, 1500, 2047, 2048])
+@pytest.mark.parametrize("lo_min", [1, 2049])
+def test_mul_lo_u64_classical_and_ntt(ctx, devmem, m, lo_min):
+    """mi_mul_lo_u64 with the low-half crossover forced to the NTT (1) and to
+    the classical kernel (2049): the same low limbs as the oracle."""
+    old = ctx.get_tuning(midint.TUNE_LO_NTT_MIN)
+    ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, lo_min)
+    try:
+        a, b = carry_stress(7, m, seed=5 * m + lo_min)
+        assert np.array_equal(gpu_mul(ctx, devmem, a, b, m, full=False), O.mul(a, b, m, False))
+        ones = np.full(3 * m, 0xFFFFFFFFFFFFFFFF, np.uint64)
+        assert np.array_equal(gpu_mul(ctx, devmem, ones, ones, m, full=False), O.mul(ones, ones, m, False))
+    finally:
+        ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, old)
+
+
+def test_lo_ntt_min_knob(ctx):
+    old = ctx.get_tuning(midint.TUNE_LO_NTT_MIN)
+    for bad in (0, 2050):
+        with pytest.raises(midint.MidintError):
+            ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, bad)
+    assert ctx.get_tuning(midint.TUNE_LO_NTT_MIN) == old
+    ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, 2049)
+    assert ctx.get_tuning(midint.TUNE_LO_NTT_MIN) == 2049
+    ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, old)
+
+
 def test_compat_gpuMultiply(lib):
     g = golden("ref_sweep.npz")
-    for m in (16, 256, 2048, 4096):
+    for m in (16, 256, 1024, 2048, 4096):  # the u64 form of the last three takes the NTT low half
         r = np.zeros_like(g["a"])
         midint.gpuMultiply(midint.U32bits, m, g["a"].size // m, g["a"], g["b"], r)
         assert np.array_equal(r, g[f"mul_{m}"])

@@ -23,6 +23,7 @@ def test_table_matches_record():
     table = _table()
     picks = json.load(open(os.path.join(PKG, "tuning.json")))["picks"]
     assert table["kPlainNttMin"] == picks["plain_ntt_min"]
+    assert table["kLoNttMin"] == picks["lo_ntt_min"]
     assert table["kRaggedNttMin"] == picks["ragged_ntt_min"]
     assert table["kAddThreadBytes"] == picks["add_thread_bytes"]
     assert table["kHostChunks"] == picks["host_chunks"]
@@ -33,6 +34,7 @@ def test_table_matches_record():
 def test_picks_are_accepted_values():
     picks = json.load(open(os.path.join(PKG, "tuning.json")))["picks"]
     assert 1 <= picks["plain_ntt_min"] <= 2049
+    assert 1 <= picks["lo_ntt_min"] <= 2049
     assert 1 <= picks["ragged_ntt_min"] <= 257
     assert len(picks["add_thread_bytes"]) == 13 and set(picks["add_thread_bytes"]) <= {16, 32, 64}
     assert all(1 <= c <= 64 for c in picks["host_chunks"])
