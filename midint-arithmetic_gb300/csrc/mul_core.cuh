@@ -318,7 +318,7 @@ __device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restri
 // zero block nb instead, which exists whenever they do.  On return thread t
 // holds output blocks t (ulo) and NH+t (uhi), fully carried; the carry out of
 // block NB-1 is dropped (the product mod 2^(32*T*NB)).
-template <int NH, int UNROLL = NH >= 16 ? 4 : 2>
+template <int NH, int UNROLL = NH >= 16 ? 8 : 2>
 __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
                                             uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                             uint32_t nb = 2 * NH) {

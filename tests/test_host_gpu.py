@@ -179,3 +179,20 @@ def test_host_tuning_knobs_are_checked(hctx):
         hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 2, 1)
     hctx.set_tuning(midint.TUNE_HOST_CHUNKS, 1, 5)
     assert hctx.get_tuning(midint.TUNE_HOST_CHUNKS, 1) == 5
+
+
+@pytest.mark.parametrize("m", [320, 512, 2048])
+def test_compat_gpuMultiply_ntt_low_half_on_pinned_buffers(lib, m):
+    """The u64 gpuMultiply wrapper takes the NTT low half from 320 limbs on;
+    on mapped pinned buffers its kernel reads and writes them in place (the
+    tuned zero-copy mode of products), on pageable ones through copies."""
+    n = 40
+    a, b = carry_stress(n, m, seed=m + 3)
+    want = O.mul(a, b, m, False)
+    pa, pb = _pinned(a), _pinned(b)
+    pr = torch.zeros(n * m, dtype=torch.int64).pin_memory()
+    midint.check(lib.mi_compat_gpuMultiply_u64(n, m, pa.data_ptr(), pb.data_ptr(), pr.data_ptr()))
+    assert np.array_equal(pr.numpy().view(np.uint64), want)
+    r = np.zeros(n * m, np.uint64)
+    midint.gpuMultiply(midint.U64bits, m, n, a, b, r)
+    assert np.array_equal(r, want)
