@@ -60,8 +60,9 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 
         classic::stage_b<NT, VEC>(gB4, b + off, n32, valid, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        if (nb == NT)  // no padding: the trip count is a compile-time constant
-            classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi, NT);
+        if (nb == NT)  // no padding: a compile-time trip count, unrolled in full for 8..32 steps
+            classic::square_product<NT, 1, (NT >= 8 && NT <= 32) ? NT : (NT >= 16 ? 8 : 2)>(gA, gB4, slots, scr, t,
+                                                                                         ulo, uhi, NT);
         else
             classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi, nb);
         if (valid) {

@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(NH > 256 ? NH : 256, 3)
         classic::stage_planes<S::NB, NH, VEC>(gB4, b + off, n32, valid, t);
         group_sync<NH>();
         uint32_t ulo[T], uhi[T];
-        if (nb == S::NB)  // no padding: the trip count is a compile-time constant
-            classic::low_product<NH>(gA4, gB4, slots, scr, t, ulo, uhi, S::NB);
+        if (nb == S::NB)  // no padding: a compile-time trip count, unrolled in full for 9..65 steps
+            classic::low_product<NH, (NH >= 4 && NH <= 32) ? 2 * NH + 1 : (NH >= 16 ? 8 : 2)>(gA4, gB4, slots, scr, t,
+                                                                                              ulo, uhi, S::NB);
         else
             classic::low_product<NH>(gA4, gB4, slots, scr, t, ulo, uhi, nb);
         if (valid) {
