@@ -350,7 +350,7 @@ def run_ours(args):
                      "unit": "G 32x32-bit partial products/s", "frac": achieved_prod / peak_prod,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one k_mul<32> launch (ncu, cold, single
                      # launch): the 32 MiB of operands read once, the product still in L2 at kernel end
-                     "traffic": 33.62e6 + 0.35e6,
+                     "traffic": 33.62e6 + 0.23e6,
                      "traffic_source": "ncu --set full of one k_mul<32> launch (summary committed under profiles/)",
                      "peak_source": "measured in-process: mi_calib_mul32_peak (independent mad.lo.cc/madc.hi.cc "
                                     "chains, the kernel's own instruction mix)",
