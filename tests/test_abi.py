@@ -79,3 +79,23 @@ def test_context_without_device_reports_enodev(lib):
     h = ctypes.c_void_p()
     st = lib.mi_ctx_create(0, ctypes.byref(h))
     assert st == midint.MI_ENODEV and h.value is None
+
+
+def test_header_constants_match_the_python_mirror():
+    """Every enumerator and numeric #define of include/midint.h that midint.py
+    mirrors has the same value there (under its own name or without MI_)."""
+    text = open(os.path.join(ROOT, "include", "midint.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    consts = {n: int(v) for n, v in re.findall(r"\b(MI_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    consts.update({n: int(v) for n, v in re.findall(r"#define\s+(MI_[A-Z0-9_]+)\s+(\d+)u?\b", text)})
+    assert "MI_TUNE_LO_NTT_MIN" in consts and "MI_OP_MUL" in consts
+    checked = 0
+    for name, value in consts.items():
+        py = [n for n in (name, name[3:]) if hasattr(midint, n)]
+        if not py:
+            continue  # a limit the mirror leaves to the C side
+        assert getattr(midint, py[0]) == value, name
+        checked += 1
+    assert checked >= 20
+    tunes = [n for n in consts if n.startswith("MI_TUNE_")]
+    assert all(hasattr(midint, n[3:]) for n in tunes)
