@@ -20,6 +20,10 @@ when --warmup 1) with seeded inputs already resident on the device:
           each pair takes 48-bit digits on four primes, the second 64-bit
           digits on five, at the same transform length), ns per product with
           CUDA events over 10 launches after 3, printed as JSON
+  ntt_batches  NTT products of 1024 u64 limbs in batches of 152..2736
+          instances (the persistent grid holds 3 groups per SM), ms per
+          launch with CUDA events over 20 launches after 3 on 3 rotating
+          operand sets, printed as JSON
   wide_variants  additions of 16 pairs x 2^21 u64 limbs with no all-ones pair,
           every 8th pair all-ones + 1, and every pair all-ones + 1 (the
           carry runs through every tile), each timed with CUDA events over
@@ -124,6 +128,8 @@ def main():
         print(json.dumps(wide_variants(ctx, dev, sp), indent=1))
     if "ntt_sizes" in ops:
         print(json.dumps(ntt_sizes(ctx, dev, sp), indent=1))
+    if "ntt_batches" in ops:
+        print(json.dumps(ntt_batches(ctx, dev, sp), indent=1))
     ctx.close()
     print("profcase: ran", ",".join(ops))
 
@@ -153,6 +159,41 @@ def ntt_sizes(ctx, dev, sp) -> dict:
         del da, db, dr
         torch.cuda.empty_cache()
     return res
+
+
+def _event_ms(fn, warmup: int, reps: int) -> float:
+    """Mean ms per call of fn(i) with CUDA events on the current stream (the
+    stream `sp` of the callers)."""
+    import torch
+
+    for i in range(warmup):
+        fn(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(reps):
+        fn(i)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def ntt_batches(ctx, dev, sp) -> dict:
+    import torch
+
+    import workloads
+
+    m, sets = 1024, 3
+    a, b = workloads.ntt_pairs(n=2736, m=m)
+    da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+    db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+    dr = [torch.empty(2 * a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    out = {}
+    for n in (152, 304, 456, 608, 760, 912, 1024, 1368, 1824, 2736):
+        ms = _event_ms(lambda i: ctx.mul_ntt(da[i % sets], db[i % sets], dr[i % sets], n, m, stream=sp), 3, 20)
+        out[str(n)] = {"ms": ms, "us_per_instance_per_sm": ms * 1e3 * sms / n}
+    return out
 
 
 def wide_variants(ctx, dev, sp) -> dict:
