@@ -95,6 +95,15 @@ def tune_add(ctx, stream, dev) -> tuple[list[int], dict]:
     return picks, record
 
 
+def crossover_pick(sizes: list[int], ntt_faster: dict[int, bool], never: int = 2049) -> int:
+    """The smallest measured size from which the NTT is faster at every larger
+    measured size, or `never` when it is not faster at the largest."""
+    for i, m in enumerate(sizes):
+        if all(ntt_faster[x] for x in sizes[i:]):
+            return m
+    return never
+
+
 def tune_plain_crossover(ctx, stream, dev) -> tuple[int, dict]:
     import torch
 
@@ -113,11 +122,7 @@ def tune_plain_crossover(ctx, stream, dev) -> tuple[int, dict]:
         ntt_faster[m] = t_ntt < t_cls
         del a, b, r
         torch.cuda.empty_cache()
-    pick = 2049
-    for i, m in enumerate(sizes):
-        if all(ntt_faster[x] for x in sizes[i:]):
-            pick = m
-            break
+    pick = crossover_pick(sizes, ntt_faster)
     return pick, record
 
 
@@ -146,11 +151,7 @@ def tune_lo_crossover(ctx, stream, dev) -> tuple[int, dict]:
         ntt_faster[m] = t["ntt"] < t["classical"]
         del a, b, r
         torch.cuda.empty_cache()
-    pick = 2049
-    for i, m in enumerate(sizes):
-        if all(ntt_faster[x] for x in sizes[i:]):
-            pick = m
-            break
+    pick = crossover_pick(sizes, ntt_faster)
     ctx.set_tuning(midint.TUNE_LO_NTT_MIN, 0, pick)
     return pick, record
 

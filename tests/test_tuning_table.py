@@ -40,3 +40,32 @@ def test_picks_are_accepted_values():
     assert all(1 <= c <= 64 for c in picks["host_chunks"])
     assert all(0 <= z <= 3 for z in picks["host_zero_copy"])
     assert all(0 <= b <= 3 for b in picks["host_zc_blocks"])
+
+
+def test_crossover_pick_rule():
+    import sys
+
+    sys.path.insert(0, PKG)
+    from autotune import crossover_pick
+
+    sizes = [64, 128, 256, 512]
+    assert crossover_pick(sizes, {64: False, 128: False, 256: True, 512: True}) == 256
+    # a faster size below a slower one does not count
+    assert crossover_pick(sizes, {64: True, 128: False, 256: True, 512: True}) == 256
+    assert crossover_pick(sizes, {64: True, 128: True, 256: True, 512: True}) == 64
+    assert crossover_pick(sizes, {64: True, 128: True, 256: True, 512: False}) == 2049
+
+
+def test_recorded_crossovers_follow_the_rule():
+    """The committed picks are what the rule gives on the committed timings."""
+    import sys
+
+    sys.path.insert(0, PKG)
+    from autotune import crossover_pick
+
+    rec = json.load(open(os.path.join(PKG, "tuning.json")))
+    for key, pick in (("plain_crossover", "plain_ntt_min"), ("lo_crossover", "lo_ntt_min")):
+        sizes = sorted(int(m) for m in rec[key])
+        faster = {m: rec[key][str(m)]["ntt_ns_per_product"] < rec[key][str(m)]["classical_ns_per_product"]
+                  for m in sizes}
+        assert crossover_pick(sizes, faster) == rec["picks"][pick], key
