@@ -10,7 +10,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "common.cuh"
 #include "ctx.h"
@@ -40,15 +43,28 @@ mi_status cuda_error(cudaError_t e, const char* what) {
 }
 
 int sm_count() {
-    static int cache[64] = {};
+    static std::atomic<int> cache[64];  // zero-initialised (static storage)
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (cache[dev] == 0) {
-        int v = 0;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
-        cache[dev] = v;
+        cache[dev].store(v, std::memory_order_relaxed);
     }
-    return cache[dev];
+    return v;
+}
+
+mi_status ensure_dyn_smem(const void* kern, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> limit;
+    int dev = 0;
+    MI_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = limit[{kern, dev}];
+    if (cur >= bytes) return MI_OK;
+    MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    cur = bytes;
+    return MI_OK;
 }
 
 }  // namespace mi

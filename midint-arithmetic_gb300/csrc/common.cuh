@@ -40,6 +40,15 @@ mi_status cuda_error(cudaError_t e, const char* what);
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Raises the dynamic shared-memory limit of kernel `kern` on the current
+// device to at least `bytes`, never lowering it; safe from several host
+// threads (one lock, a per-kernel-and-device record of the limit set).
+mi_status ensure_dyn_smem(const void* kern, size_t bytes);
+template <typename K>
+inline mi_status ensure_dyn_smem(K* kern, size_t bytes) {
+    return ensure_dyn_smem(reinterpret_cast<const void*>(kern), bytes);
+}
+
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 inline bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
 

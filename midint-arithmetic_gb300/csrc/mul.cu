@@ -95,16 +95,9 @@ mi_status launch_nt(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t 
                     cudaStream_t st, uint32_t max_per_sm) {
     using S = MulShape<NT>;
     auto kern = k_mul<NT, VEC>;
-    static size_t attr_bytes[64] = {};  // the kernel's dynamic shared-memory limit, per device
-    int dev = 0;
-    MI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return set_error(MI_ENODEV, "device %d out of range", dev);
     size_t smem = S::SMEM;
     MI_TRY(capped_smem(S::SMEM, max_per_sm, &smem));
-    if (attr_bytes[dev] < smem) {
-        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        attr_bytes[dev] = smem;
-    }
+    MI_TRY(ensure_dyn_smem(kern, smem));
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
     const uint64_t cap = uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;

@@ -21,18 +21,12 @@ struct LoShape {
 using LoKernel = void (*)(const uint32_t*, const uint32_t*, uint32_t*, uint32_t, uint32_t);
 
 // Launches kern (a low-half kernel with NH threads per instance, which starts
-// with pdl_wait) with launch_pdl; attr_done is the caller's per-device flag
-// for the shared-memory opt-in.
+// with pdl_wait) with launch_pdl.
 template <int NH>
-mi_status launch_lo(LoKernel kern, bool* attr_done, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n,
-                    uint32_t n32, cudaStream_t st) {
+mi_status launch_lo(LoKernel kern, const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32,
+                    cudaStream_t st) {
     using S = LoShape<NH>;
-    int dev = 0;
-    MI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-        attr_done[dev] = true;
-    }
+    MI_TRY(ensure_dyn_smem(kern, S::SMEM));
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
     const uint64_t cap = uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;

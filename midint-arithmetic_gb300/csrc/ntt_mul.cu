@@ -60,13 +60,7 @@ mi_status launch_lg(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t 
                     const NttMulParams& P, cudaStream_t st) {
     using S = NttShape<LG>;
     auto kern = k_ntt_mul<LG, NP>;
-    static bool attr_done[64] = {};
-    int dev = 0;
-    MI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        MI_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-        attr_done[dev] = true;
-    }
+    MI_TRY(ensure_dyn_smem(kern, S::SMEM));
     int per_sm = 0;
     MI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::NT, S::SMEM));
     uint64_t blocks = uint64_t(sm_count()) * (per_sm > 0 ? per_sm : 1);

@@ -145,11 +145,8 @@ __global__ void __launch_bounds__(NH > 256 ? NH : 256, 2)
 template <bool VEC>
 mi_status dispatch(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, cudaStream_t st) {
     switch (lo_threads(n32)) {
-#define MI_LO_CASE(NH)                                                                   \
-    case NH: {                                                                           \
-        static bool attr_done[64] = {};                                                  \
-        return launch_lo<NH>(k_poly<NH, VEC>, attr_done, a, b, r, n, n32, st);           \
-    }
+#define MI_LO_CASE(NH) \
+    case NH: return launch_lo<NH>(k_poly<NH, VEC>, a, b, r, n, n32, st);
         MI_LO_CASE(1) MI_LO_CASE(2) MI_LO_CASE(4) MI_LO_CASE(8) MI_LO_CASE(16) MI_LO_CASE(32) MI_LO_CASE(64)
         MI_LO_CASE(128) MI_LO_CASE(256)
 #undef MI_LO_CASE

@@ -196,3 +196,40 @@ def test_compat_gpuMultiply_ntt_low_half_on_pinned_buffers(lib, m):
     r = np.zeros(n * m, np.uint64)
     midint.gpuMultiply(midint.U64bits, m, n, a, b, r)
     assert np.array_equal(r, want)
+
+
+def test_contexts_on_several_host_threads(lib):
+    """Host threads with their own contexts and different zero-copy occupancy
+    caps (different shared-memory requests of the same product kernel) call
+    at once; every result is the oracle's."""
+    import threading
+
+    n, m = 600, 128
+    a, b = carry_stress(n, m, seed=404)
+    want = O.mul(a, b, m, True)
+    pa, pb = _pinned(a), _pinned(b)
+    outs = [torch.zeros(2 * n * m, dtype=torch.int64).pin_memory() for _ in range(4)]
+    ctxs = [midint.Context(0) for _ in range(4)]
+    errors = []
+    start = threading.Barrier(4)
+
+    def run(i):
+        try:
+            ctxs[i].set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 1)
+            ctxs[i].set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, i)
+            start.wait()
+            for _ in range(3):
+                ctxs[i].host_mul_full(pa, pb, outs[i], n, m)
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for c in ctxs:
+        c.close()
+    assert not errors, errors
+    for o in outs:
+        assert np.array_equal(o.numpy().view(np.uint64), want)
