@@ -117,6 +117,14 @@ def job_rate(world: int, units_per_rank: int, max_ms: float) -> float:
     return world * units_per_rank / (max_ms * 1e-3)
 
 
+def hbm_position(bytes_per_launch: int, ms: float, peak_gbs) -> dict:
+    """Where a launch that moves `bytes_per_launch` in `ms` sits against the
+    measured HBM bandwidth (for kernels bound elsewhere: shows the distance)."""
+    gbs = bytes_per_launch / (ms * 1e-3) / 1e9
+    return {"achieved": gbs, "peak": peak_gbs, "unit": "GB/s", "bytes_per_launch": bytes_per_launch,
+            "frac": (gbs / peak_gbs) if peak_gbs else None}
+
+
 # --- clocks ----------------------------------------------------------------------
 
 class ClockSampler:
@@ -354,7 +362,9 @@ def run_ours(args):
                      "traffic_source": "ncu --set full of one k_mul<32> launch (summary committed under profiles/)",
                      "peak_source": "measured in-process: mi_calib_mul32_peak (independent mad.lo.cc/madc.hi.cc "
                                     "chains, the kernel's own instruction mix)",
-                     "per_unit": f"{prods32_per_inst} partial products per instance"},
+                     "per_unit": f"{prods32_per_inst} partial products per instance",
+                     # operands in and products out once: far below the HBM bound
+                     "hbm": hbm_position(4 * in_bytes, ms, measured_peaks().get("hbm_gbs"))},
         "gpu_launches": args.steps,
         "clocks": clk,
         "e2e": e2e,
