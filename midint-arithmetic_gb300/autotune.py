@@ -283,6 +283,17 @@ constexpr uint32_t kHostZcBlocks[2] = {{{zc_blocks}}};
 """
 
 
+def render_header(device: str, date: str, picks: dict) -> str:
+    """csrc/tuning_table.h for the given picks."""
+    def join(xs):
+        return ", ".join(str(x) for x in xs)
+
+    return HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], lo=picks["lo_ntt_min"],
+                         ragged=picks["ragged_ntt_min"], chunks=join(picks["host_chunks"]),
+                         zero_copy=join(picks["host_zero_copy"]), zc_blocks=join(picks["host_zc_blocks"]),
+                         add=join(picks["add_thread_bytes"]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out-dir", default=".")
@@ -321,12 +332,7 @@ def main():
     ctx.close()
     device = torch.cuda.get_device_name(0)
     date = datetime.date.today().isoformat()
-    header = HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], lo=picks["lo_ntt_min"],
-                           ragged=picks["ragged_ntt_min"],
-                           chunks=", ".join(str(x) for x in picks["host_chunks"]),
-                           zero_copy=", ".join(str(x) for x in picks["host_zero_copy"]),
-                           zc_blocks=", ".join(str(x) for x in picks["host_zc_blocks"]),
-                           add=", ".join(str(x) for x in picks["add_thread_bytes"]))
+    header = render_header(device, date, picks)
     record = {"device": device, "date": date, "torch": torch.__version__, "measured": sorted(only),
               "picks": picks, **record}
     if args.apply:

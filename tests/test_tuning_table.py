@@ -69,3 +69,16 @@ def test_recorded_crossovers_follow_the_rule():
         faster = {m: rec[key][str(m)]["ntt_ns_per_product"] < rec[key][str(m)]["classical_ns_per_product"]
                   for m in sizes}
         assert crossover_pick(sizes, faster) == rec["picks"][pick], key
+
+
+def test_header_is_what_the_tuner_writes():
+    """csrc/tuning_table.h is byte for byte the tuner's template filled with
+    the committed record (no hand edits)."""
+    import sys
+
+    sys.path.insert(0, PKG)
+    import autotune
+
+    rec = json.load(open(os.path.join(PKG, "tuning.json")))
+    header = autotune.render_header(rec["device"], rec["date"], rec["picks"])
+    assert open(os.path.join(PKG, "csrc", "tuning_table.h")).read() == header
