@@ -24,8 +24,11 @@ A step is one batched multiplication over the whole batch.
 oracle's port of gmpAddMulOnce over GMP; the reference's own build cannot run
 on an Arm GPU host) on the same workload with all host threads.
 
-Multi-GPU (torchrun, N>1): every rank multiplies its own batch (instances are
-independent, no collective on the data path); max-over-ranks time.
+Multi-GPU (N>1): one rank per GPU under torchrun (`--gpus N` without a
+launcher re-executes itself under torch.distributed.run).  Every rank
+multiplies its own contiguous range of the job's instances (instances are
+independent, no collective on the data path); the ragged list of the whole
+job is split across ranks by estimated work; max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -48,6 +51,7 @@ N_MUL, M_MUL = 16384, 128
 N_ADD, M_ADD = 65536, 64
 L2_BYTES = 129 * 1024 * 1024
 CHECK_N = 256  # instances of the timed batch cross-checked against the CPU baseline
+SERVE_FIXED_RATE = 4000.0  # requests/s: the serving row's fixed offered load
 
 
 def parse():
@@ -110,6 +114,57 @@ def max_over_ranks(world, x: float) -> float:
 def rank_seed(base: int, rank: int) -> int:
     """Seed of a rank's own batch: ranks process disjoint instances (weak scaling)."""
     return base + 1000 * rank
+
+
+def instance_range(n_per_rank: int, rank: int) -> tuple[int, int]:
+    """The instances [lo, hi) of the whole job's batch that a rank processes:
+    contiguous ranges of equal size (instances are independent, so the batch
+    shards without any exchange)."""
+    return rank * n_per_rank, (rank + 1) * n_per_rank
+
+
+def launch_command(args_argv: list[str], gpus: int, port: int) -> list[str]:
+    """The torchrun command that runs this bench with one rank per GPU of one
+    node; the ranks read RANK / LOCAL_RANK / WORLD_SIZE from the environment."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *args_argv]
+
+
+def check_world(gpus: int, world: int) -> str | None:
+    """'launch' when --gpus asks for more ranks than the environment has and
+    no launcher started this process; an error message when a launcher
+    started a different number of ranks; None when they agree."""
+    if gpus == world:
+        return None
+    if world == 1 and "WORLD_SIZE" not in os.environ:
+        return "launch"
+    return f"--gpus {gpus} but the launcher started {world} ranks"
+
+
+def ragged_work_estimate(kind: np.ndarray, la: np.ndarray, lb: np.ndarray) -> np.ndarray:
+    """Estimated device seconds of each ragged op, for splitting a list across
+    ranks: additions move 3 x 8 bytes per limb at about 6.5 TB/s; products
+    cost the cheaper of the classical form (4 la lb partial products at about
+    7e12/s) and an NTT of the next power of two of la + lb u64 digits (about
+    97 ns per 2048-point product, scaled by L log L)."""
+    la = la.astype(np.float64)
+    lb = lb.astype(np.float64)
+    add = 24.0 * np.maximum(la, lb) / 6.5e12
+    L = np.maximum(256.0, 2.0 ** np.ceil(np.log2(la + lb)))
+    ntt = 97e-9 * (L / 2048.0) * (np.log2(L) / 11.0)
+    mul = np.minimum(4.0 * la * lb / 7e12, ntt)
+    return np.where(kind == 0, add, mul)
+
+
+def shard_ragged(work: np.ndarray, world: int) -> list[np.ndarray]:
+    """Splits a ragged list across ranks by estimated work: ops in descending
+    cost are dealt to ranks in snake order (0..w-1, w-1..0, ...), so every
+    rank gets about the same total; each rank's indices come back in list
+    order.  Every op lands on exactly one rank."""
+    order = np.argsort(-work, kind="stable")
+    pos = np.arange(order.size) % (2 * world)
+    owner = np.where(pos < world, pos, 2 * world - 1 - pos)
+    return [np.sort(order[owner == r]) for r in range(world)]
 
 
 def job_rate(world: int, units_per_rank: int, max_ms: float) -> float:
@@ -251,6 +306,48 @@ def measured_peaks() -> dict:
         return {}
 
 
+def link_rates(dev, in_bufs: list[int], out_bufs: list[int], reps: int = 10) -> dict:
+    """Host-link rates with pinned host memory: one cudaMemcpyAsync per
+    buffer (the sizes of the e2e step's own operand and result buffers),
+    host->device alone, device->host alone, and both directions at once on
+    two streams.  GB/s of bytes moved, best of `reps`, CUDA events."""
+    import torch
+
+    h_in = [torch.empty(n, dtype=torch.uint8).pin_memory() for n in in_bufs]
+    d_in = [torch.empty(n, dtype=torch.uint8, device=dev) for n in in_bufs]
+    h_out = [torch.empty(n, dtype=torch.uint8).pin_memory() for n in out_bufs]
+    d_out = [torch.empty(n, dtype=torch.uint8, device=dev) for n in out_bufs]
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(h2d: bool, d2h: bool) -> float:
+        best = float("inf")
+        for _ in range(reps + 2):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s1)
+            s2.wait_event(e0)
+            if h2d:
+                with torch.cuda.stream(s1):
+                    for d, h in zip(d_in, h_in):
+                        d.copy_(h, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(s2):
+                    for h, d in zip(h_out, d_out):
+                        h.copy_(d, non_blocking=True)
+            s1.wait_stream(s2)
+            e1.record(s1)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    bi, bo = sum(in_bufs), sum(out_bufs)
+    t_in, t_out, t_both = timed(True, False), timed(False, True), timed(True, True)
+    return {"h2d_gbs": bi / (t_in * 1e-3) / 1e9, "d2h_gbs": bo / (t_out * 1e-3) / 1e9,
+            "both_gbs": (bi + bo) / (t_both * 1e-3) / 1e9, "both_ms": t_both,
+            "how": f"pinned cudaMemcpyAsync, one per buffer ({len(in_bufs)} x {in_bufs[0] >> 20} MiB in, "
+                   f"{len(out_bufs)} x {out_bufs[0] >> 20} MiB out), best of {reps}, CUDA events"}
+
+
 def run_ours(args):
     import torch
 
@@ -265,7 +362,7 @@ def run_ours(args):
     sp = stream.cuda_stream
 
     # --- headline: classical multiplication, device-resident operands ---------
-    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, first=instance_range(N_MUL, rank)[0])
     in_bytes = a.nbytes
     set_bytes = 2 * in_bytes + 2 * in_bytes
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
@@ -327,9 +424,14 @@ def run_ours(args):
             2: "mi_host_mul_full_u64 on pinned host buffers; the kernels read the operands in place over the host "
                "link while the products of earlier chunks are copied out (the tuned choice for multiplications)"
             }[zero_copy]
+    # the link's own rate on the step's buffers: the floor of an end-to-end step
+    link = link_rates(dev, [in_bytes, in_bytes], [2 * in_bytes])
     e2e = {"value": world * N_MUL / e2e_s, "unit": "products/s", "h2d_bytes_per_step": 2 * in_bytes,
            "d2h_bytes_per_step": 2 * in_bytes, "ms_per_step": e2e_s * 1e3, "path": path,
-           "copy_pipeline_ms_per_step": copy_s * 1e3}
+           "copy_pipeline_ms_per_step": copy_s * 1e3,
+           # bytes across the link per step over the step time, against both directions busy at once
+           "link_gbs": link["both_gbs"], "frac_link": (4 * in_bytes) / e2e_s / 1e9 / link["both_gbs"],
+           "link": link}
     del da, db, dr
     torch.cuda.empty_cache()
 
@@ -374,10 +476,47 @@ def run_ours(args):
         a_cpu, b_cpu = workloads.mul_pairs(n=N_MUL, m=M_MUL)
         out["cpu_baseline"] = dict(cpu_baseline(a_cpu, b_cpu, M_MUL, args.cpu_seconds, "mul", check=got),
                                    unit="products/s")
+        # last key of the line, compact: the targets of every benchmark row
+        out["targets"] = targets(out, extra)
         print(json.dumps(out))
         if out["cpu_baseline"].get("matches_gpu_first_instances") is False:
             raise SystemExit("bench: GPU products differ from the CPU baseline's")
     ctx.close()
+
+
+def _r(x, nd=4):
+    return None if x is None else round(float(x), nd)
+
+
+def targets(out: dict, extra: dict) -> dict:
+    """One compact object with each benchmark row's position against its
+    target: the classical headline against the IMAD ceiling, 4096-bit
+    addition against HBM (>= 0.80), the NTT product against the IMAD ceiling,
+    the ragged list against the plain per-size-class form (>= 2.0, results
+    identical), serving p50/p99 at the fixed offered load, and the
+    end-to-end call against the host link."""
+    t = {"mul_8192bit": {"frac": _r(out["roofline"]["frac"]), "ms_per_launch": _r(out["ms_per_step"], 5)},
+         "e2e": {"frac_link": _r(out["e2e"].get("frac_link")), "link_gbs": _r(out["e2e"].get("link_gbs"), 1)}}
+    if "add_4096bit" in extra:
+        a = extra["add_4096bit"]
+        t["add_4096bit"] = {"frac_hbm": _r(a["roofline"]["frac"]), "ms_per_launch": _r(a["ms_per_launch"], 5),
+                            "target": 0.80}
+    if "ntt_mul_65536bit" in extra:
+        n = extra["ntt_mul_65536bit"]
+        t["ntt_mul_65536bit"] = {"frac": _r(n["roofline"]["frac"]), "ms_per_launch": _r(n["ms_per_launch"], 5)}
+    if "ragged_200k" in extra:
+        g = extra["ragged_200k"]
+        t["ragged"] = {"vs_plain": _r(g["ragged_vs_plain"], 3), "ragged_ms": _r(g["ragged_ms"], 4),
+                       "results_identical": g["results_identical"], "target": 2.0}
+    if "serving" in extra and extra["serving"].get("fixed_load"):
+        f = extra["serving"]["fixed_load"]
+        t["serving"] = {"offered_req/s": f["offered_req/s"],
+                        "batched_p50_p99_ms": [_r(f["batched"]["p50_ms"], 3), _r(f["batched"]["p99_ms"], 3)],
+                        "per_request_p50_p99_ms": [_r(f["per_request"]["p50_ms"], 3),
+                                                   _r(f["per_request"]["p99_ms"], 3)]}
+    if "fused" in extra and "poly_2048limb" in extra["fused"]:
+        t["poly_131072bit"] = {"ms_per_launch": _r(extra["fused"]["poly_2048limb"]["ms_per_launch"], 4)}
+    return t
 
 
 def secondary_workloads(args, ctx, dev, stream, world, rank) -> dict:
@@ -431,7 +570,7 @@ def size_sweep(args, ctx, dev, stream, world, rank) -> dict:
     for m32 in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096):
         m = m32 // 2  # u64 limbs
         n = total // m32
-        a, b = workloads.mul_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 9, rank) + m32)
+        a, b = workloads.mul_pairs(n=n, m=m, seed=workloads.SEED_BASE + 9 + m32, first=instance_range(n, rank)[0])
         with torch.cuda.stream(stream):
             da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(2)]
             db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(2)]
@@ -463,7 +602,7 @@ def add_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     hbm = measured_peaks().get("hbm_gbs")
-    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=rank_seed(workloads.SEED_BASE, rank))
+    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, first=instance_range(N_ADD, rank)[0])
     set_bytes = 3 * a.nbytes + N_ADD
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
     with torch.cuda.stream(stream):
@@ -508,7 +647,7 @@ def ntt_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     n_ntt, m_ntt = 1024, 1024
-    a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, seed=rank_seed(workloads.SEED_BASE + 2, rank))
+    a, b = workloads.ntt_pairs(n=n_ntt, m=m_ntt, first=instance_range(n_ntt, rank)[0])
     set_bytes = 4 * a.nbytes
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
     with torch.cuda.stream(stream):
@@ -548,7 +687,7 @@ def u32_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     # u32-limb variant of the classical multiplication (same bytes, 256 u32 limbs)
-    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, first=instance_range(N_MUL, rank)[0])
     set_bytes = 4 * a.nbytes  # a, b and the 2m-limb product
     sets = max(2, -(-4 * L2_BYTES // set_bytes))
     with torch.cuda.stream(stream):
@@ -576,7 +715,7 @@ def wide_section(args, ctx, dev, stream, world, rank) -> dict:
     sp = stream.cuda_stream
     hbm = measured_peaks().get("hbm_gbs")
     n, m = 16, 1 << 21
-    a, b = workloads.add_pairs(n=n, m=m, seed=rank_seed(workloads.SEED_BASE + 7, rank), worst_every=8)
+    a, b = workloads.add_pairs(n=n, m=m, seed=workloads.SEED_BASE + 7, worst_every=8, first=instance_range(n, rank)[0])
     with torch.cuda.stream(stream):
         da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(2)]
         db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(2)]
@@ -605,7 +744,7 @@ def fused_section(args, ctx, dev, stream, world, rank) -> dict:
 
     sp = stream.cuda_stream
     hbm = measured_peaks().get("hbm_gbs")
-    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, seed=rank_seed(workloads.SEED_BASE, rank))
+    a, b = workloads.add_pairs(n=N_ADD, m=M_ADD, first=instance_range(N_ADD, rank)[0])
     sets = max(2, -(-4 * L2_BYTES // (3 * a.nbytes)))
     with torch.cuda.stream(stream):
         da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
@@ -617,7 +756,7 @@ def fused_section(args, ctx, dev, stream, world, rank) -> dict:
         max(args.warmup, 5), stream))
     gbs = N_ADD * 3 * M_ADD * 8 / (ms6 * 1e-3) / 1e9
     del da, db, dr
-    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, seed=rank_seed(workloads.SEED_BASE + 1, rank))
+    a, b = workloads.mul_pairs(n=N_MUL, m=M_MUL, first=instance_range(N_MUL, rank)[0])
     sets = max(2, -(-4 * L2_BYTES // (3 * a.nbytes)))
     with torch.cuda.stream(stream):
         da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
@@ -656,7 +795,7 @@ def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     import workloads
     from plainform import PlainBatch
 
-    ops, pool, out_limbs = workloads.ragged_ops(n_ops=args.ragged_ops, seed=rank_seed(workloads.SEED_BASE + 3, rank))
+    ops, pool, out_limbs = ragged_shard(args.ragged_ops, world, rank)
     n = ops.size
     sp = stream.cuda_stream
     with torch.cuda.stream(stream):
@@ -691,16 +830,39 @@ def ragged_vs_plain(args, ctx, dev, stream, world, rank) -> dict:
     torch.cuda.empty_cache()
     if not same:
         raise SystemExit("bench: ragged and plain-form results differ")
+    total = args.ragged_ops * world
     return {
-        "config": f"{n} ops, 40% add / 60% mul, operand bits log-uniform in [256, 65536] (4..1024 u64 limbs), "
-                  "independent lengths; adds return max(la,lb) limbs + carry, muls la+lb limbs",
-        "ragged_ms": ms_r, "ragged_ops/s": world * n / (ms_r * 1e-3),
-        "plain_ms": ms_p, "plain_ops/s": world * n / (ms_p * 1e-3), "plain_launches": launches[0],
+        "config": f"{total} ops, 40% add / 60% mul, operand bits log-uniform in [256, 65536] (4..1024 u64 limbs), "
+                  "independent lengths; adds return max(la,lb) limbs + carry, muls la+lb limbs"
+                  + (f"; split over {world} ranks by estimated work ({n} ops on rank {rank})" if world > 1 else ""),
+        "ragged_ms": ms_r, "ragged_ops/s": total / (ms_r * 1e-3),
+        "plain_ms": ms_p, "plain_ops/s": total / (ms_p * 1e-3), "plain_launches": launches[0],
         "ragged_vs_plain": ms_p / ms_r,
         "mul_partial_products": int((la[muls] * lb[muls]).sum() * 4),
         "results_identical": same, "invalid_ops": invalid,
         "ragged_path": "one CUDA graph: classify, scan, scatter, persistent NTT / classical / add kernels",
     }
+
+
+def ragged_shard(n_per_rank: int, world: int, rank: int):
+    """This rank's part of the whole job's ragged list of n_per_rank x world
+    ops: the kinds and lengths are drawn for the whole list from one seed
+    (the same on every rank), split by estimated work (shard_ragged), and
+    the rank's ops are packed with seeded operands of their own.  With one
+    rank this is exactly workloads.ragged_ops(n_per_rank)."""
+    import workloads
+
+    seed = workloads.SEED_BASE + 3
+    total = n_per_rank * world
+    rng = np.random.default_rng(seed)
+    kind = (rng.random(total) >= 0.4).astype(np.uint32)
+    lo, hi = np.log(256), np.log(65536)
+    la = np.ceil(np.exp(rng.uniform(lo, hi, total)) / 64).astype(np.uint32)
+    lb = np.ceil(np.exp(rng.uniform(lo, hi, total)) / 64).astype(np.uint32)
+    if world == 1:
+        return workloads.pack_ops(kind, la, lb, seed)
+    mine = shard_ragged(ragged_work_estimate(kind, la, lb), world)[rank]
+    return workloads.pack_ops(kind[mine], la[mine], lb[mine], rank_seed(seed, rank))
 
 
 def make_requests(count: int, seed: int):
@@ -762,6 +924,10 @@ def serving_sweep(args, ctx, rank) -> dict:
         out["sweep"].append({"load_fraction_of_batched_capacity": frac,
                              "batched": serve_once(ctx, reqs, rate, True, 2),
                              "per_request": serve_once(ctx, reqs, rate, False, 2)})
+    # one named offered load, the same in every run
+    out["fixed_load"] = {"offered_req/s": SERVE_FIXED_RATE,
+                         "batched": serve_once(ctx, reqs, SERVE_FIXED_RATE, True, 3),
+                         "per_request": serve_once(ctx, reqs, SERVE_FIXED_RATE, False, 3)}
     return out
 
 
@@ -813,6 +979,19 @@ def run_reference(args):
 
 def main():
     args = parse()
+    world, _, _ = dist_env()
+    verdict = check_world(args.gpus, world)
+    if verdict == "launch":
+        # --gpus N without a launcher: start N local ranks under torchrun
+        import socket
+
+        s = socket.socket()
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+        s.close()
+        raise SystemExit(subprocess.call(launch_command(sys.argv[1:], args.gpus, port)))
+    if verdict is not None:
+        raise SystemExit(f"bench: {verdict}")
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -27,25 +27,27 @@ _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
 
 
-def splitmix64(seed: int, count: int) -> np.ndarray:
-    """The first `count` outputs of splitmix64 started at `seed`."""
+def splitmix64(seed: int, count: int, start: int = 0) -> np.ndarray:
+    """Outputs start .. start+count-1 of splitmix64 started at `seed`."""
     with np.errstate(over="ignore"):
-        x = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + _GOLD * np.arange(1, count + 1, dtype=np.uint64)
+        x = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + _GOLD * np.arange(start + 1, start + count + 1, dtype=np.uint64)
         z = (x ^ (x >> np.uint64(30))) * _M1
         z = (z ^ (z >> np.uint64(27))) * _M2
         return z ^ (z >> np.uint64(31))
 
 
-def uniform(n: int, m: int, seed: int) -> np.ndarray:
-    return splitmix64(seed, n * m)
+def uniform(n: int, m: int, seed: int, first: int = 0) -> np.ndarray:
+    """Instances first .. first+n-1 (m limbs each) of one seeded stream."""
+    return splitmix64(seed, n * m, first * m)
 
 
-def add_pairs(n: int = 65536, m: int = 64, seed: int = SEED_BASE + 0, worst_every: int = 8):
-    """Addition workload: (a, b) flat u64 arrays of n*m limbs."""
-    a = uniform(n, m, seed)
-    b = uniform(n, m, seed ^ 0xB0B0B0B0)
+def add_pairs(n: int = 65536, m: int = 64, seed: int = SEED_BASE + 0, worst_every: int = 8, first: int = 0):
+    """Addition workload: (a, b) flat u64 arrays of n*m limbs (instances
+    first .. first+n-1 of the seeded batch)."""
+    a = uniform(n, m, seed, first)
+    b = uniform(n, m, seed ^ 0xB0B0B0B0, first)
     if worst_every:
-        rows = np.arange(0, n, worst_every)
+        rows = np.arange((-first) % worst_every, n, worst_every)
         a2, b2 = a.reshape(n, m), b.reshape(n, m)
         a2[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
         b2[rows, :] = 0
@@ -53,17 +55,19 @@ def add_pairs(n: int = 65536, m: int = 64, seed: int = SEED_BASE + 0, worst_ever
     return a, b
 
 
-def mul_pairs(n: int = 16384, m: int = 128, seed: int = SEED_BASE + 1):
-    """Classical-multiplication workload: uniform (a, b) of n*m u64 limbs."""
-    return uniform(n, m, seed), uniform(n, m, seed ^ 0xB0B0B0B0)
+def mul_pairs(n: int = 16384, m: int = 128, seed: int = SEED_BASE + 1, first: int = 0):
+    """Classical-multiplication workload: uniform (a, b) of n*m u64 limbs
+    (instances first .. first+n-1 of the seeded batch)."""
+    return uniform(n, m, seed, first), uniform(n, m, seed ^ 0xB0B0B0B0, first)
 
 
-def ntt_pairs(n: int = 1024, m: int = 1024, seed: int = SEED_BASE + 2, ones_every: int = 16):
-    """NTT-multiplication workload: uniform, every 16th pair all ones."""
-    a = uniform(n, m, seed)
-    b = uniform(n, m, seed ^ 0xB0B0B0B0)
+def ntt_pairs(n: int = 1024, m: int = 1024, seed: int = SEED_BASE + 2, ones_every: int = 16, first: int = 0):
+    """NTT-multiplication workload: uniform, every 16th pair all ones
+    (instances first .. first+n-1 of the seeded batch)."""
+    a = uniform(n, m, seed, first)
+    b = uniform(n, m, seed ^ 0xB0B0B0B0, first)
     if ones_every:
-        rows = np.arange(0, n, ones_every)
+        rows = np.arange((-first) % ones_every, n, ones_every)
         a.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
         b.reshape(n, m)[rows, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
     return a, b
