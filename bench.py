@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU-baseline sample budget")
     ap.add_argument("--ragged-ops", type=int, default=200000, help="ops in the ragged batch")
+    ap.add_argument("--case", default=None,
+                    help="profiling cases instead of the bench (comma list; see run_case): one launch of each "
+                         "named kernel family, or a timing scan")
+    ap.add_argument("--case-warmup", type=int, default=1, help="untimed calls before a case's launches")
+    ap.add_argument("--case-ragged-ops", type=int, default=20000, help="ops in the ragged case's list")
     ap.add_argument("--sections", default="add,ntt,ragged,serving,u32,fused,wide",
                     help="secondary workloads to run (comma list of add, ntt, ragged, serving, u32, fused, wide; "
                          "sweep, the reference driver's size sweep, runs only when named)")
@@ -771,6 +776,32 @@ def fused_section(args, ctx, dev, stream, world, rank) -> dict:
         max(args.warmup, 3), stream))
     del da, db, dr
     torch.cuda.empty_cache()
+    # the composite at 131072 bits: the transform form (the tuned choice at this
+    # size) and the classical form, on the same operands
+    import midint
+
+    n2, m2 = 512, 2048
+    a, b = workloads.mul_pairs(n=n2, m=m2, seed=workloads.SEED_BASE + 11, first=instance_range(n2, rank)[0])
+    sets = max(2, -(-4 * L2_BYTES // (3 * a.nbytes)))
+    with torch.cuda.stream(stream):
+        da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+        db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+        dr = [torch.empty(a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    torch.cuda.synchronize()
+    old = ctx.get_tuning(midint.TUNE_POLY_NTT_MIN)
+    ms2 = max_over_ranks(world, time_device(
+        lambda i: ctx.poly(da[i], db[i], dr[i], n2, m2, stream=sp), sets, max(10, args.steps // 2),
+        max(args.warmup, 3), stream))
+    out_ntt = dr[0].cpu()
+    ctx.set_tuning(midint.TUNE_POLY_NTT_MIN, 0, 2049)
+    ms2c = max_over_ranks(world, time_device(
+        lambda i: ctx.poly(da[i], db[i], dr[i], n2, m2, stream=sp), sets, 3, 1, stream))
+    ctx.set_tuning(midint.TUNE_POLY_NTT_MIN, 0, old)
+    same2 = bool(torch.equal(out_ntt, dr[0].cpu()))  # set 0 ran in both forms
+    del da, db, dr
+    torch.cuda.empty_cache()
+    if not same2:
+        raise SystemExit("bench: the two forms of the composite differ")
     return {
         "add6": {"config": "6a + 10b mod 2^4096, 65536 pairs x 64 u64 limbs (the addition workload)",
                  "ms_per_launch": ms6, "instances/s": world * N_ADD / (ms6 * 1e-3), "GB/s": world * gbs,
@@ -781,6 +812,12 @@ def fused_section(args, ctx, dev, stream, world, rank) -> dict:
         "mul_lo": {"config": "low 8192 bits of the product, 16384 pairs x 128 u64 limbs (the reference's "
                              "gpuMultiply semantics); anti-diagonals below the middle only",
                    "ms_per_launch": mslo, "products/s": world * N_MUL / (mslo * 1e-3)},
+        "poly_2048limb": {"config": f"((a^2 + b)(b^2 + b) + ab) mod 2^131072, {n2} pairs x {m2} u64 limbs; four "
+                                    "low-half products on number-theoretic transforms (from the tuned crossover, "
+                                    f"{old} limbs), intermediates in shared memory",
+                          "ms_per_launch": ms2, "instances/s": world * n2 / (ms2 * 1e-3),
+                          "classical_form_ms_per_launch": ms2c, "ntt_vs_classical": ms2c / ms2,
+                          "results_identical": same2},
     }
 
 
@@ -977,6 +1014,258 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+# --- profiling cases -----------------------------------------------------------
+
+def run_case(args):
+    """Profiling cases (--case): one launch of each named kernel family on the
+    benchmark's shapes, inputs resident on cuda:0, after --case-warmup untimed
+    calls, so that a profiler can capture exactly those launches; or one of
+    the timing scans, printed as JSON.  Prints no bench line.
+
+      add     65536 x 64 u64 limbs, carries        (k_add)
+      add6    6a + 10b on the same batch            (k_add, 6a+10b variant)
+      mul     16384 x 128 u64 limbs, full products  (k_mul)
+      mul_lo  the same batch, low halves            (k_mul_lo)
+      poly    the same batch                        (k_poly)
+      poly2048  512 x 2048 u64 limbs, the composite on transforms (k_poly_ntt)
+      ntt     1024 x 1024 u64 limbs                 (k_ntt_mul, 64-bit digits on five primes)
+      ntt48   1024 x 768 u64 limbs                  (k_ntt_mul, 48-bit digits on four primes, L = 2048)
+      ragged  a mixed ragged list (--case-ragged-ops)  (k_classify, k_scan, k_scatter, k_rg_*)
+      wide    16 pairs x 2^21 u64 limbs             (k_add_wide)
+      convert the addition batch to big-endian 8-byte words and back (k_export, k_count_words, k_import)
+      ragged_bands  the ragged list cut into its additions and its products by
+              shorter-operand band, each band timed alone as its own captured
+              ragged run (CUDA events over 10 replays after 3)
+      ntt_sizes  NTT products at 384/400, 768/800 and 1536/1600 limbs (48-bit
+              digits on four primes against 64-bit digits on five at the same
+              transform length), ns per product, CUDA events over 10 after 3
+      ntt_batches  NTT products of 1024 u64 limbs in batches of 152..2736
+              instances, ms per launch, CUDA events over 20 after 3
+      wide_variants  16 pairs x 2^21 u64 limbs with no all-ones pair, every
+              8th pair all-ones + 1, and every pair all-ones + 1, GB/s
+    """
+    import torch
+
+    import midint
+    import workloads
+
+    dev = torch.device("cuda:0")
+    ctx = midint.Context(0)
+    sp = torch.cuda.current_stream().cuda_stream
+
+    def dput(x):
+        return torch.from_numpy(x.view(np.int64)).to(dev)
+
+    calls = []
+    ops = args.case.split(",")
+    if "add" in ops or "add6" in ops or "convert" in ops:
+        a, b = workloads.add_pairs(n=65536, m=64)
+        da, db = dput(a), dput(b)
+        dr = torch.empty_like(da)
+        dc = torch.empty(65536, dtype=torch.uint8, device=dev)
+        if "add" in ops:
+            calls.append(lambda: ctx.add(da, db, dr, 65536, 64, carry=dc, stream=sp))
+        if "add6" in ops:
+            calls.append(lambda: ctx.add6(da, db, dr, 65536, 64, stream=sp))
+        if "convert" in ops:
+            cw = torch.empty(65536, dtype=torch.int32, device=dev)
+            calls.append(lambda: ctx.export_words(da, 65536, 64, dr, 64, 8, 1, 1, counts=cw, stream=sp))
+            calls.append(lambda: ctx.import_words(dr, 65536, 64, 8, 1, 1, db, 64, stream=sp))
+    if any(o in ops for o in ("mul", "mul_lo", "poly")):
+        a, b = workloads.mul_pairs(n=16384, m=128)
+        ma, mb = dput(a), dput(b)
+        mr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        if "mul" in ops:
+            calls.append(lambda: ctx.mul_full(ma, mb, mr, 16384, 128, stream=sp))
+        if "mul_lo" in ops:
+            calls.append(lambda: ctx.mul_lo(ma, mb, mr, 16384, 128, stream=sp))
+        if "poly" in ops:
+            calls.append(lambda: ctx.poly(ma, mb, mr, 16384, 128, stream=sp))
+    if "poly2048" in ops:
+        a2, b2 = workloads.mul_pairs(n=512, m=2048, seed=workloads.SEED_BASE + 11)
+        pa, pb = dput(a2), dput(b2)
+        pr = torch.empty(a2.size, dtype=torch.int64, device=dev)
+        calls.append(lambda: ctx.poly(pa, pb, pr, 512, 2048, stream=sp))
+    if "ntt" in ops:
+        a, b = workloads.ntt_pairs(n=1024, m=1024)
+        na, nb = dput(a), dput(b)
+        nr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        calls.append(lambda: ctx.mul_ntt(na, nb, nr, 1024, 1024, stream=sp))
+    if "ntt48" in ops:
+        a4, b4 = workloads.ntt_pairs(n=1024, m=768)
+        qa, qb = dput(a4), dput(b4)
+        qr = torch.empty(2 * a4.size, dtype=torch.int64, device=dev)
+        calls.append(lambda: ctx.mul_ntt(qa, qb, qr, 1024, 768, stream=sp))
+    if "wide" in ops:
+        wa, wb = workloads.add_pairs(n=16, m=1 << 21, worst_every=8)
+        xa, xb = dput(wa), dput(wb)
+        xr = torch.empty_like(xa)
+        xc = torch.empty(16, dtype=torch.uint8, device=dev)
+        calls.append(lambda: ctx.add(xa, xb, xr, 16, 1 << 21, carry=xc, stream=sp))
+    if "ragged" in ops:
+        rops, pool, out_limbs = workloads.ragged_ops(n_ops=args.case_ragged_ops)
+        d_ops = torch.from_numpy(rops.view(np.uint8).copy()).to(dev)
+        d_in = dput(pool)
+        d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+        d_c = torch.empty(rops.size, dtype=torch.uint8, device=dev)
+        sb = midint.ragged_scratch_bytes(rops.size)
+        scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+        calls.append(lambda: ctx.ragged_run(d_ops, rops.size, d_in, d_out, scr, sb, carry=d_c, stream=sp))
+    torch.cuda.synchronize()
+    for _ in range(args.case_warmup):
+        for c in calls:
+            c()
+    torch.cuda.synchronize()
+    for c in calls:
+        c()
+    torch.cuda.synchronize()
+    if "ragged_bands" in ops:
+        print(json.dumps(case_ragged_bands(ctx, dev, sp, args.case_ragged_ops), indent=1))
+    if "wide_variants" in ops:
+        print(json.dumps(case_wide_variants(ctx, dev, sp), indent=1))
+    if "ntt_sizes" in ops:
+        print(json.dumps(case_ntt_sizes(ctx, dev, sp), indent=1))
+    if "ntt_batches" in ops:
+        print(json.dumps(case_ntt_batches(ctx, dev, sp), indent=1))
+    ctx.close()
+    print("case: ran", ",".join(ops))
+
+
+def case_ntt_sizes(ctx, dev, sp) -> dict:
+    """ns per NTT product at sizes either side of the 48-bit digit limit."""
+    import torch
+
+    import workloads
+
+    res = {}
+    for m in (384, 400, 768, 800, 1536, 1600):
+        n = 2048 * 1024 // m  # about 2^21 limbs per operand array
+        a, b = workloads.ntt_pairs(n=n, m=m)
+        da = torch.from_numpy(a.view(np.int64)).to(dev)
+        db = torch.from_numpy(b.view(np.int64)).to(dev)
+        dr = torch.empty(2 * a.size, dtype=torch.int64, device=dev)
+        for _ in range(3):
+            ctx.mul_ntt(da, db, dr, n, m, stream=sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ctx.mul_ntt(da, db, dr, n, m, stream=sp)
+        e1.record()
+        e1.synchronize()
+        res[str(m)] = {"instances": n, "ns_per_product": e0.elapsed_time(e1) / 10 * 1e6 / n}
+        del da, db, dr
+        torch.cuda.empty_cache()
+    return res
+
+
+def _event_ms(fn, warmup: int, reps: int) -> float:
+    """Mean ms per call of fn(i) with CUDA events on the current stream (the
+    stream `sp` of the callers)."""
+    import torch
+
+    for i in range(warmup):
+        fn(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(reps):
+        fn(i)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def case_ntt_batches(ctx, dev, sp) -> dict:
+    import torch
+
+    import workloads
+
+    m, sets = 1024, 3
+    a, b = workloads.ntt_pairs(n=2736, m=m)
+    da = [torch.from_numpy(a.view(np.int64)).to(dev) for _ in range(sets)]
+    db = [torch.from_numpy(b.view(np.int64)).to(dev) for _ in range(sets)]
+    dr = [torch.empty(2 * a.size, dtype=torch.int64, device=dev) for _ in range(sets)]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    out = {}
+    for n in (152, 304, 456, 608, 760, 912, 1024, 1368, 1824, 2736):
+        ms = _event_ms(lambda i: ctx.mul_ntt(da[i % sets], db[i % sets], dr[i % sets], n, m, stream=sp), 3, 20)
+        out[str(n)] = {"ms": ms, "us_per_instance_per_sm": ms * 1e3 * sms / n}
+    return out
+
+
+def case_wide_variants(ctx, dev, sp) -> dict:
+    """16 x 2^21-limb additions with 0, 1/8 and all pairs carrying through."""
+    import torch
+
+    import workloads
+
+    n, m = 16, 1 << 21
+    res = {}
+    for name, worst in (("uniform", 0), ("every 8th all-ones", 8), ("all all-ones", 1)):
+        a, b = workloads.add_pairs(n=n, m=m, worst_every=worst)
+        da = torch.from_numpy(a.view(np.int64)).to(dev)
+        db = torch.from_numpy(b.view(np.int64)).to(dev)
+        dr = torch.empty_like(da)
+        dc = torch.empty(n, dtype=torch.uint8, device=dev)
+        for _ in range(3):
+            ctx.add(da, db, dr, n, m, carry=dc, stream=sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ctx.add(da, db, dr, n, m, carry=dc, stream=sp)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        res[name] = {"ms": ms, "GB/s": (3 * n * m * 8 + n) / ms / 1e6}
+        del da, db, dr
+        torch.cuda.empty_cache()
+    res["device_status"] = ctx.device_status()
+    return res
+
+
+# (name, kind, lowest shorter-operand limbs, highest) of each band
+BANDS = (("adds", 0, 1, 1024), ("mul 1..8", 1, 1, 8), ("mul 9..16", 1, 9, 16), ("mul 17..32", 1, 17, 32),
+         ("mul 33..64", 1, 33, 64), ("mul 65..127", 1, 65, 127), ("mul >=128", 1, 128, 1024))
+
+
+def case_ragged_bands(ctx, dev, sp, n_ops: int) -> dict:
+    """Each band of the ragged list run alone: ops, ms per run and the
+    32x32-bit partial products of the classical product per second."""
+    import torch
+
+    import midint
+    import workloads
+
+    rops, _, _ = workloads.ragged_ops(n_ops=n_ops)
+    kind, la, lb = rops["kind"], rops["la"], rops["lb"]
+    short = np.minimum(la, lb)
+    res = {}
+    for name, k, lo, hi in (("all", -1, 1, 1024),) + BANDS:
+        sel = (short >= lo) & (short <= hi) & ((kind == k) if k >= 0 else True)
+        o, pool, out_limbs = workloads.pack_ops(kind[sel].astype(np.uint32), la[sel].astype(np.uint32),
+                                                lb[sel].astype(np.uint32), workloads.SEED_BASE + 5)
+        d_ops = torch.from_numpy(o.view(np.uint8).copy()).to(dev)
+        d_in = torch.from_numpy(pool.view(np.int64)).to(dev)
+        d_out = torch.empty(out_limbs, dtype=torch.int64, device=dev)
+        d_c = torch.empty(o.size, dtype=torch.uint8, device=dev)
+        sb = midint.ragged_scratch_bytes(o.size)
+        scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device=dev)
+        g = ctx.ragged_graph(d_ops, o.size, d_in, d_out, scr, sb, carry=d_c)
+        for _ in range(3):
+            g.launch(sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            g.launch(sp)
+        e1.record()
+        e1.synchronize()
+        g.close()
+        ms = e0.elapsed_time(e1) / 10
+        pp = int((4 * la[sel].astype(np.int64) * lb[sel].astype(np.int64) * (kind[sel] == 1)).sum())
+        res[name] = {"ops": int(sel.sum()), "ms": ms, "G_pp_per_s": pp / ms / 1e6}
+    return res
+
+
 def main():
     args = parse()
     world, _, _ = dist_env()
@@ -992,6 +1281,9 @@ def main():
         raise SystemExit(subprocess.call(launch_command(sys.argv[1:], args.gpus, port)))
     if verdict is not None:
         raise SystemExit(f"bench: {verdict}")
+    if args.case:
+        run_case(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

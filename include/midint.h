@@ -134,7 +134,11 @@ enum {
                                    * multiplication kernel (0: as many as fit).
                                    * Fewer resident blocks make the first
                                    * results leave over the host link sooner */
-    MI_TUNE_LO_NTT_MIN = 9
+    MI_TUNE_LO_NTT_MIN = 9,
+    MI_TUNE_POLY_NTT_MIN = 10     /* cls ignored; value 1..2049: mi_poly_u64
+                                   * runs its four products on number-theoretic
+                                   * transforms from this many limbs on
+                                   * (2049 = never) */
 };
 mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value);
 
@@ -191,7 +195,10 @@ mi_status mi_mul_full_u32(mi_ctx ctx, const uint32_t* a, const uint32_t* b, uint
 
 /* Fused polynomial composite r = ((a^2 + b)(b^2 + b) + ab) mod 2^(64*limbs),
  * every intermediate mod 2^(64*limbs) and held on chip, limbs <= 2048.
- * Replaces polyKerQ (cuda/ker-classic-mul.cu.h:500-575). */
+ * Replaces polyKerQ (cuda/ker-classic-mul.cu.h:500-575), four classical
+ * low-half products, and from MI_TUNE_POLY_NTT_MIN limbs on polyFttKer
+ * (cuda/ker-fft-mul.cu.h:456-509), the same four products on exact
+ * number-theoretic transforms; the result is the same either way. */
 mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
                       uint32_t n, uint32_t limbs, mi_stream stream);
 
@@ -229,7 +236,10 @@ mi_status mi_export_words(mi_ctx ctx, const uint64_t* src, uint32_t n, uint32_t 
  * (cuda/ker-fft-mul.cu.h:427-454) as launched by gpuMulFFT
  * (cuda/main.cu:415-520); unlike it, the result is exact at every size.
  * mi_mul_u64 picks the classical or the NTT kernel by size.
- * r must not overlap a or b.
+ * r must not overlap a or b.  mi_mul_ntt_u64 needs 8-byte aligned buffers
+ * (MI_EINVAL otherwise); mi_mul_u64, mi_mul_lo_u64 and mi_poly_u64 use the
+ * transforms only for 8-byte aligned buffers and the classical kernels
+ * (which read 32-bit words) for the others.
  * ------------------------------------------------------------------------- */
 mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r,
                          uint32_t n, uint32_t limbs, mi_stream stream);
@@ -284,7 +294,7 @@ mi_status mi_host_mul_full_u64(mi_ctx ctx, const uint64_t* h_a, const uint64_t* 
  * output pool: an add writes max(la, lb) limbs (the sum modulo 2^(64 max))
  * and, if carry_out is given, carry_out[op index]; a multiply writes la + lb
  * limbs (the full product).  1 <= la, lb <= 1024.  Results must not overlap
- * each other or the inputs.  Ops with a bad kind or length are skipped and
+ * each other or the inputs.  ops, in and out must be 8-byte aligned.  Ops with a bad kind or length are skipped and
  * counted (mi_ragged_invalid).
  * ------------------------------------------------------------------------- */
 #define MI_OP_ADD 0u
@@ -325,10 +335,18 @@ mi_status mi_ragged_invalid(const void* scratch, uint32_t* count);
  * (and loads the size-class tables); make it before capturing any stream.
  * All calls share the array, so calls whose work overlaps on the GPU race:
  * order them on one stream.  The context is created beforehand as usual.
+ * The array's device address is looked up once per device and kept for the
+ * life of the process, so the library is not usable on a device after a
+ * cudaDeviceReset there (its contexts are not either).
  * No counterpart in the reference. */
 #define MI_RAGGED_NOALLOC_MAX_OPS 65536u
 mi_status mi_ragged_run_noalloc(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
                                 uint8_t* carry_out, mi_stream stream);
+
+/* Number of ops the last mi_ragged_run_noalloc on the context's device
+ * skipped as invalid, read from the static array (synchronous, allocates
+ * nothing).  No counterpart in the reference. */
+mi_status mi_ragged_invalid_noalloc(mi_ctx ctx, uint32_t* count);
 
 /* The same run captured once into a CUDA graph and replayed. */
 typedef struct mi_graph_s* mi_graph;
@@ -388,17 +406,39 @@ mi_status mi_server_stats(mi_server server, uint64_t* batches, uint64_t* request
 mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s, double* seconds);
 
 /* ---------------------------------------------------------------------------
- * One NTT on a single prime, run by the same transform code as the
- * multiplication kernels: conv = 0 gives the forward transform of `a` in
- * natural order (the reference's fft, cuda/ker-fft-mul.cu.h:304-348), conv = 1
- * the cyclic convolution of a and b mod p (bmulFFTvalid,
+ * One NTT on a single caller-chosen prime, in 64-bit Montgomery fields (a
+ * separate radix-8 transform, csrc/ntt.cuh, that can run the reference's own
+ * primes; the multiplication kernels use the 30-bit transform of
+ * mi_ntt32_raw below): conv = 0 gives the forward transform of `a` in natural
+ * order (the reference's fft, cuda/ker-fft-mul.cu.h:304-348), conv = 1 the
+ * cyclic convolution of a and b mod p (bmulFFTvalid,
  * cuda/ker-fft-mul.cu.h:512-554).  p odd < 2^62, g of order 2^two_adicity
  * (two_adicity >= 12), len a power of two in [8, 2048]; host buffers of len
- * words; synchronous.  Used to check the transform against the reference's
- * known answers.
+ * words; synchronous.  Used to check a transform of the reference's shape
+ * against the reference's known answers.
  * ------------------------------------------------------------------------- */
 mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, uint32_t len, int conv,
                      const uint64_t* h_a, const uint64_t* h_b, uint64_t* h_out);
+
+/* ---------------------------------------------------------------------------
+ * The transform that the NTT multiplication kernels run (csrc/ntt32.cuh), on
+ * its own, on production prime number `prime` (0..4, the five 30-bit primes
+ * of mi_ntt32_prime) with the context's resident twiddles: conv = 0 gives the
+ * forward transform of `a` in natural order, X_k = sum_i a_i w^(ik) mod p with
+ * w = g^((p-1)/len); conv = 1 the cyclic convolution of a and b mod p, by the
+ * same per-prime steps as a multiplication (scaled conversions, lockstep
+ * forward transforms, Montgomery pointwise product, inverse transform).
+ * Replaces the role of the reference's fft / bmulFFTvalid
+ * (cuda/ker-fft-mul.cu.h:304-348, 512-554) as the transform-level check.
+ * len a power of two in [256, 4096]; inputs are reduced mod p; host buffers
+ * of len words; synchronous.
+ * ------------------------------------------------------------------------- */
+mi_status mi_ntt32_raw(mi_ctx ctx, uint32_t prime, uint32_t len, int conv, const uint32_t* h_a,
+                       const uint32_t* h_b, uint32_t* h_out);
+
+/* Prime number `prime` (0..4) of the NTT multiplication kernels and its
+ * primitive root. */
+mi_status mi_ntt32_prime(uint32_t prime, uint32_t* p, uint32_t* g);
 
 #ifdef __cplusplus
 }

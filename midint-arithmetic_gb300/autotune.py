@@ -14,6 +14,8 @@ Knobs:
     products from 64 to 1024 u64 limbs; the crossover is the smallest measured
     size from which the NTT is faster at every larger measured size;
   * the same for the low half (mi_mul_lo_u64), 256 to 2048 limbs;
+  * the same for the fused composite (mi_poly_u64: four classical low halves
+    against four low halves on transforms), 64 to 2048 limbs;
   * ragged classical/NTT crossover: the 200000-op mixed ragged workload (40%
     adds, operand bits log-uniform in [256, 65536]) timed end to end for every
     candidate threshold; the fastest wins;
@@ -156,6 +158,40 @@ def tune_lo_crossover(ctx, stream, dev) -> tuple[int, dict]:
     return pick, record
 
 
+def tune_poly_crossover(ctx, stream, dev) -> tuple[int, dict]:
+    """The fused composite ((a^2 + b)(b^2 + b) + ab) mod 2^(64m) through
+    mi_poly_u64, classical (the knob at 2049) against the transform form (the
+    knob at 1), from 64 to 2048 u64 limbs, picked as for the plain crossover;
+    the two forms' results are compared."""
+    import torch
+
+    import midint
+
+    sizes = [64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 1024, 1536, 2048]
+    record, ntt_faster = {}, {}
+    sp = stream.cuda_stream
+    for m in sizes:
+        n = max(256, (64 << 20) // (8 * m))
+        a = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        b = torch.randint(-2**62, 2**62, (n * m,), dtype=torch.int64, device=dev)
+        r = torch.empty(n * m, dtype=torch.int64, device=dev)
+        t, outs = {}, {}
+        for name, knob in (("classical", 2049), ("ntt", 1)):
+            ctx.set_tuning(midint.TUNE_POLY_NTT_MIN, 0, knob)
+            t[name] = _timer(lambda: ctx.poly(a, b, r, n, m, stream=sp), 3, 1, stream)
+            outs[name] = r.cpu()
+        if not torch.equal(outs["classical"], outs["ntt"]):
+            raise SystemExit(f"autotune: the two poly forms differ at {m} limbs")
+        record[str(m)] = {"instances": n, "classical_ns_per_instance": t["classical"] * 1e6 / n,
+                          "ntt_ns_per_instance": t["ntt"] * 1e6 / n}
+        ntt_faster[m] = t["ntt"] < t["classical"]
+        del a, b, r
+        torch.cuda.empty_cache()
+    pick = crossover_pick(sizes, ntt_faster)
+    ctx.set_tuning(midint.TUNE_POLY_NTT_MIN, 0, pick)
+    return pick, record
+
+
 def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
     import torch
 
@@ -262,6 +298,9 @@ constexpr uint32_t kPlainNttMin = {plain};
 // mi_mul_lo_u64: low halves of products of at least this many u64 limbs come
 // from the NTT kernel (2049 = never).
 constexpr uint32_t kLoNttMin = {lo};
+// mi_poly_u64: composites of at least this many u64 limbs run their four
+// products on the NTT (2049 = never).
+constexpr uint32_t kPolyNttMin = {poly};
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = {ragged};
@@ -289,6 +328,7 @@ def render_header(device: str, date: str, picks: dict) -> str:
         return ", ".join(str(x) for x in xs)
 
     return HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], lo=picks["lo_ntt_min"],
+                         poly=picks["poly_ntt_min"],
                          ragged=picks["ragged_ntt_min"], chunks=join(picks["host_chunks"]),
                          zero_copy=join(picks["host_zero_copy"]), zc_blocks=join(picks["host_zc_blocks"]),
                          add=join(picks["add_thread_bytes"]))
@@ -299,7 +339,8 @@ def main():
     ap.add_argument("--out-dir", default=".")
     ap.add_argument("--apply", action="store_true", help="write into the package (csrc/, tuning.json)")
     ap.add_argument("--ragged-ops", type=int, default=200000)
-    ap.add_argument("--only", default="add,plain,lo,ragged,host", help="knob groups to measure (others keep the table)")
+    ap.add_argument("--only", default="add,plain,lo,poly,ragged,host",
+                    help="knob groups to measure (others keep the table)")
     args = ap.parse_args()
 
     import torch
@@ -318,13 +359,17 @@ def main():
     picks.setdefault("host_zero_copy", [0, 1])
     picks.setdefault("host_zc_blocks", [0, 0])
     picks.setdefault("lo_ntt_min", 2049)
-    record = {k: old.get(k) for k in ("add", "plain_crossover", "lo_crossover", "ragged_crossover", "host")}
+    picks.setdefault("poly_ntt_min", 2049)
+    record = {k: old.get(k) for k in ("add", "plain_crossover", "lo_crossover", "poly_crossover", "ragged_crossover",
+                                      "host")}
     if "add" in only:
         picks["add_thread_bytes"], record["add"] = tune_add(ctx, stream, dev)
     if "plain" in only:
         picks["plain_ntt_min"], record["plain_crossover"] = tune_plain_crossover(ctx, stream, dev)
     if "lo" in only:
         picks["lo_ntt_min"], record["lo_crossover"] = tune_lo_crossover(ctx, stream, dev)
+    if "poly" in only:
+        picks["poly_ntt_min"], record["poly_crossover"] = tune_poly_crossover(ctx, stream, dev)
     if "ragged" in only:
         picks["ragged_ntt_min"], record["ragged_crossover"] = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
     if "host" in only:

@@ -132,7 +132,10 @@ mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n,
         return set_error(MI_EINVAL, "mul: result overlaps an operand");
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
-    if (pick_ntt && !full && limb_bytes == 8 && limbs >= ctx->lo_ntt_min && limbs <= kNttMaxLimbs)
+    // (the NTT kernels read 8-byte words: rows that are only 4-byte aligned
+    // take the classical kernel, which reads 32-bit words)
+    if (pick_ntt && !full && limb_bytes == 8 && limbs >= ctx->lo_ntt_min && limbs <= kNttMaxLimbs &&
+        aligned8(a) && aligned8(b) && aligned8(r))
         return launch_mul_ntt(static_cast<const uint64_t*>(a), static_cast<const uint64_t*>(b),
                               static_cast<uint64_t*>(r), n, limbs, ctx->ntt.params, pick_stream(ctx, stream), true);
     const uint32_t n32 = limbs * uint32_t(limb_bytes / 4);
@@ -143,6 +146,7 @@ mi_status mul_any(mi_ctx ctx, const void* a, const void* b, void* r, uint32_t n,
 mi_status mul_ntt(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                   mi_stream stream) {
     MI_TRY(check_batch(a, b, r, limbs, kNttMaxLimbs, "mul_ntt"));
+    if (!aligned8(a) || !aligned8(b) || !aligned8(r)) return set_error(MI_EINVAL, "mul_ntt: buffers not 8-byte aligned");
     const size_t in_bytes = size_t(n) * limbs * 8;
     if (n > 0 && (any_overlap(r, 2 * in_bytes, a, in_bytes) || any_overlap(r, 2 * in_bytes, b, in_bytes)))
         return set_error(MI_EINVAL, "mul_ntt: result overlaps an operand");
@@ -181,7 +185,12 @@ mi_status ensure_stage(mi_ctx ctx, size_t bytes) {
 }
 
 // The device address of a mapped pinned host buffer, or null.
+// The device address of a mapped pinned host buffer that kernels may read or
+// write in place, or null.  Buffers that are not 8-byte aligned are not used
+// in place (the staging buffers of the copy path are): the u64 and NTT
+// kernels read whole 8-byte words.
 void* mapped_host(const void* p) {
+    if (!aligned8(p)) return nullptr;
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
         cudaGetLastError();
@@ -431,6 +440,11 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
                 return set_error(MI_EINVAL, "lo_ntt_min %u outside 1..%u", value, kNttMaxLimbs + 1);
             ctx->lo_ntt_min = value;
             return MI_OK;
+        case MI_TUNE_POLY_NTT_MIN:
+            if (value < 1 || value > kNttMaxLimbs + 1)
+                return set_error(MI_EINVAL, "poly_ntt_min %u outside 1..%u", value, kNttMaxLimbs + 1);
+            ctx->poly_ntt_min = value;
+            return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:
             if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
             if (value != 16 && value != 32 && value != 64)
@@ -475,6 +489,7 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
         case MI_TUNE_PLAIN_NTT_MIN: *value = ctx->plain_ntt_min; return MI_OK;
         case MI_TUNE_RAGGED_NTT_MIN: *value = ctx->ragged_ntt_min; return MI_OK;
         case MI_TUNE_LO_NTT_MIN: *value = ctx->lo_ntt_min; return MI_OK;
+        case MI_TUNE_POLY_NTT_MIN: *value = ctx->poly_ntt_min; return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:
             if (cls > 12) return set_error(MI_EINVAL, "addition size class %u outside 0..12", cls);
             *value = ctx->add_thread_bytes[cls];
@@ -534,6 +549,10 @@ mi_status mi_poly_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t
         return set_error(MI_EINVAL, "poly: result overlaps an operand");
     if (n == 0) return MI_OK;
     MI_TRY(check_ctx(ctx));
+    // from the tuned crossover on, the four products run on transforms (the
+    // reference's polyFttKer); below it, the classical form (polyKerQ)
+    if (limbs >= ctx->poly_ntt_min && aligned8(a) && aligned8(b) && aligned8(r))
+        return launch_poly_ntt(a, b, r, n, limbs, ctx->ntt.params, pick_stream(ctx, stream));
     return launch_poly(reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b),
                        reinterpret_cast<uint32_t*>(r), n, 2 * limbs, pick_stream(ctx, stream));
 }
@@ -584,7 +603,8 @@ mi_status mi_mul_ntt_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint6
 mi_status mi_mul_u64(mi_ctx ctx, const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t limbs,
                      mi_stream stream) {
     if (ctx == nullptr) return set_error(MI_EINVAL, "null context");
-    if (limbs >= ctx->plain_ntt_min && limbs <= kNttMaxLimbs) return mul_ntt(ctx, a, b, r, n, limbs, stream);
+    if (limbs >= ctx->plain_ntt_min && limbs <= kNttMaxLimbs && aligned8(a) && aligned8(b) && aligned8(r))
+        return mul_ntt(ctx, a, b, r, n, limbs, stream);
     return mul_any(ctx, a, b, r, n, limbs, stream, 8, true);
 }
 
@@ -623,7 +643,8 @@ mi_status mi_compat_gpuMultiply_u64(int num_instances, uint32_t m, const uint64_
     mi_ctx ctx;
     MI_TRY(default_ctx(&ctx));
     const size_t row = size_t(m) * 8;
-    const bool ntt = m >= ctx->lo_ntt_min && m <= kNttMaxLimbs;  // as mi_mul_lo_u64 picks
+    const bool ntt = m >= ctx->lo_ntt_min && m <= kNttMaxLimbs;  // as mi_mul_lo_u64 picks (the buffers the
+                                                                  // kernels see are 8-byte aligned)
     return host_pipeline(ctx, HOST_MUL, h_as, h_bs, h_rs, nullptr, uint32_t(num_instances), row, row,
                          [ctx, m, ntt](void* da, void* db, void* dr, uint8_t*, uint32_t cnt, cudaStream_t st,
                                        uint32_t cap) {
@@ -679,6 +700,8 @@ mi_status mi_ragged_scratch_bytes(uint32_t n_ops, size_t* bytes) {
 mi_status mi_ragged_run(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint64_t* in, uint64_t* out,
                         uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_stream stream) {
     if (n_ops == 0) return MI_OK;
+    if (!aligned8(ops) || !aligned8(in) || !aligned8(out))
+        return set_error(MI_EINVAL, "ragged_run: ops, in and out must be 8-byte aligned");
     MI_TRY(check_ctx(ctx));
     return ragged_launch(ctx, ops, n_ops, in, out, carry_out, scratch, scratch_bytes, ctx->ragged_ntt_min,
                          pick_stream(ctx, stream));
@@ -695,6 +718,8 @@ mi_status mi_ragged_graph_create(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, c
                                  uint8_t* carry_out, void* scratch, size_t scratch_bytes, mi_graph* graph) {
     if (graph == nullptr) return set_error(MI_EINVAL, "ragged_graph_create: null out");
     *graph = nullptr;
+    if (!aligned8(ops) || !aligned8(in) || !aligned8(out))
+        return set_error(MI_EINVAL, "ragged_graph_create: ops, in and out must be 8-byte aligned");
     MI_TRY(check_ctx(ctx));
     MI_TRY(ragged_prepare());  // constant tables and attributes, outside the capture
     cudaStream_t cs = nullptr;

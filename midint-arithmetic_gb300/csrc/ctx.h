@@ -36,6 +36,8 @@ struct mi_ctx_s {
     // mi_mul_lo_u64 and the u64 gpuMultiply wrapper: low halves of products
     // of at least this many u64 limbs come from the NTT kernel
     uint32_t lo_ntt_min = mi::tuned::kLoNttMin;
+    // mi_poly_u64: composites of at least this many u64 limbs run on the NTT
+    uint32_t poly_ntt_min = mi::tuned::kPolyNttMin;
     // multi-block additions: tile status words, counter and error word
     mi::WideState wide;
     // addition: operand bytes per thread by size class ceil(log2(u64 limbs))

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ctx.h"
 #include "kernels.h"
 #include "ntt.cuh"
 #include "ntt32.cuh"
@@ -103,6 +104,8 @@ mi_status ntt_tables_create(NttTables* T) {
         }
         P.kb[q][0] = shoup_pair(r32, p);
         P.kb[q][1] = shoup_pair(r64, p);
+        P.kone[q][0] = shoup_pair(1, p);
+        P.kone[q][1] = shoup_pair(r32, p);
     }
     int c = 0;
     for (int i = 1; i < 5; ++i)
@@ -180,4 +183,45 @@ extern "C" mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, ui
     }
     cudaFree(d);
     return st;
+}
+
+extern "C" mi_status mi_ntt32_raw(mi_ctx ctx, uint32_t prime, uint32_t len, int conv, const uint32_t* h_a,
+                                  const uint32_t* h_b, uint32_t* h_out) {
+    if (ctx == nullptr) return set_error(MI_EINVAL, "ntt32_raw: null context");
+    if (h_a == nullptr || h_out == nullptr || (conv && h_b == nullptr)) return set_error(MI_EINVAL, "ntt32_raw: null");
+    if (prime >= 5) return set_error(MI_EINVAL, "ntt32_raw: prime index %u not below 5", prime);
+    if (len < 256 || len > 4096 || (len & (len - 1)))
+        return set_error(MI_EINVAL, "ntt32_raw: length %u not a power of two in [256, 4096]", len);
+    int cur = -1;
+    MI_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != ctx->device) MI_CUDA_TRY(cudaSetDevice(ctx->device));
+    const uint32_t p = kNttPrimes[prime].p;
+    std::vector<uint32_t> ha(len), hb(len, 0);
+    for (uint32_t i = 0; i < len; ++i) ha[i] = h_a[i] % p;
+    if (conv)
+        for (uint32_t i = 0; i < len; ++i) hb[i] = h_b[i] % p;
+    uint32_t* d = nullptr;
+    MI_CUDA_TRY(cudaMalloc(&d, sizeof(uint32_t) * 3 * size_t(len)));
+    uint32_t *da = d, *db = d + len, *dout = d + 2 * len;
+    mi_status st = MI_OK;
+    cudaError_t e = cudaMemcpy(da, ha.data(), sizeof(uint32_t) * len, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, hb.data(), sizeof(uint32_t) * len, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        st = cuda_error(e, "ntt32_raw copy-in");
+    } else {
+        st = launch_ntt32_raw(da, db, dout, len, prime, conv, ctx->ntt.params, nullptr);
+        if (st == MI_OK) {
+            e = cudaMemcpy(h_out, dout, sizeof(uint32_t) * len, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) st = cuda_error(e, "ntt32_raw copy-out");
+        }
+    }
+    cudaFree(d);
+    return st;
+}
+
+extern "C" mi_status mi_ntt32_prime(uint32_t prime, uint32_t* p, uint32_t* g) {
+    if (prime >= 5 || p == nullptr || g == nullptr) return set_error(MI_EINVAL, "ntt32_prime: bad argument");
+    *p = kNttPrimes[prime].p;
+    *g = kNttPrimes[prime].g;
+    return MI_OK;
 }

@@ -27,6 +27,7 @@ struct NttMulParams {
     uint32_t pinv[5];             // -p^-1 mod 2^32
     uint2 ka_by_lg[5][5][2];      // a's conversion for L = 2^(8+i): (L^-1, 2^32 L^-1) mod p
     uint2 kb[5][2];               // b's conversion: (2^32, 2^64) mod p
+    uint2 kone[5][2];             // conversion by 1: (1, 2^32) mod p
     uint2 garner[10];             // p_k^-1 mod p_i, for i = 1..4, k = 0..i-1
     const uint2* tw[5];           // (w^e, companion), w of order 4096, in ntt32::TwLayout order
     const uint2* itw[5];          // (w^-e, companion), the same layout
@@ -61,6 +62,17 @@ struct NttRawArgs {
     int generic;
 };
 mi_status launch_ntt_raw(const NttRawArgs& A, cudaStream_t st);
+
+// ((a^2 + b)(b^2 + b) + ab) mod 2^(64m) per instance on the transforms above
+// (poly_ntt.cu), m <= kNttMaxLimbs.
+mi_status launch_poly_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t m,
+                          const NttMulParams& P, cudaStream_t st);
+
+// One forward transform (conv = 0) or cyclic convolution (conv = 1) of
+// length len (256..4096) on production prime `prime` (< 5) by the transform
+// code of the multiplication kernels; device buffers of len residues < p.
+mi_status launch_ntt32_raw(const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t len, uint32_t prime,
+                           int conv, const NttMulParams& P, cudaStream_t st);
 
 // Host modular arithmetic (exact, 128-bit intermediates).  The raw transform
 // path (mi_ntt_raw) keeps 64-bit fields so it can run the reference's own

@@ -111,6 +111,46 @@ __global__ void k_ntt_raw(const uint64_t* __restrict__ a, const uint64_t* __rest
     for (int j = 0; j < 8; ++j) out[t + Pl::NT * j] = ntt::reduce1(f.mul(x[j], 1), f.p);
 }
 
+// --- raw transforms on one of the five production primes ------------------
+// The transform code of the multiplication kernels (ntt32.cuh) on its own,
+// one block of L/8 threads: conv = 0 the forward transform of `a` (residues
+// < p) written in natural order, conv = 1 the cyclic convolution of a and b
+// mod p (a scaled by L^-1 and b by 2^32 with Shoup products, both forward
+// transforms in lockstep, the Montgomery pointwise product, the unscaled
+// inverse) -- exactly the per-prime steps of ntt32::mul_one.
+template <int LG>
+__global__ void __launch_bounds__((1 << LG) / 8)
+    k_ntt32_raw(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ out,
+                NttMulParams P, int q, int conv) {
+    using Pl = ntt32::Plan<LG>;
+    __shared__ __align__(16) uint32_t sh[2 * Pl::L];
+    const uint32_t t = threadIdx.x;
+    const ntt32::Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
+    if (!conv) {
+        uint32_t x[1][8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[0][j] = a[t + Pl::NT * j];
+        ntt32::forward<LG, 1>(x, sh, P.tw[q], f);
+        // stride-1 layout: slot 8t+j holds spectrum entry bitrev(8t+j)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[__brev(8 * t + j) >> (32 - LG)] = f.reduce(x[0][j]);
+        return;
+    }
+    const uint2 ka = P.ka_by_lg[q][LG - 8][0], kb = P.kb[q][0];
+    uint32_t x[2][8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        x[0][j] = f.shoup(a[t + Pl::NT * j], ka);
+        x[1][j] = f.shoup(b[t + Pl::NT * j], kb);
+    }
+    ntt32::forward<LG, 2>(x, sh, P.tw[q], f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[0][j] = f.mont(x[0][j], x[1][j]);
+    ntt32::inverse<LG>(x[0], sh, P.itw[q], f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) out[t + Pl::NT * j] = f.reduce(x[0][j]);
+}
+
 }  // namespace
 
 mi_status launch_mul_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t m,
@@ -159,6 +199,21 @@ mi_status launch_ntt_raw(const NttRawArgs& A, cudaStream_t st) {
         default: return set_error(MI_EINVAL, "ntt_raw: length %u not a power of two in [8, 2048]", L);
     }
 #undef RAW_CASE
+    MI_CUDA_TRY(cudaGetLastError());
+    return MI_OK;
+}
+
+mi_status launch_ntt32_raw(const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t len, uint32_t prime,
+                           int conv, const NttMulParams& P, cudaStream_t st) {
+    const int q = int(prime), c = conv ? 1 : 0;
+    switch (len) {
+        case 256: k_ntt32_raw<8><<<1, 32, 0, st>>>(a, b, out, P, q, c); break;
+        case 512: k_ntt32_raw<9><<<1, 64, 0, st>>>(a, b, out, P, q, c); break;
+        case 1024: k_ntt32_raw<10><<<1, 128, 0, st>>>(a, b, out, P, q, c); break;
+        case 2048: k_ntt32_raw<11><<<1, 256, 0, st>>>(a, b, out, P, q, c); break;
+        case 4096: k_ntt32_raw<12><<<1, 512, 0, st>>>(a, b, out, P, q, c); break;
+        default: return set_error(MI_EINVAL, "ntt32_raw: length %u not a power of two in [256, 4096]", len);
+    }
     MI_CUDA_TRY(cudaGetLastError());
     return MI_OK;
 }

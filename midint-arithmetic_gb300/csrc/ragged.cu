@@ -767,6 +767,8 @@ extern "C" mi_status mi_ragged_run_noalloc(mi_ctx ctx, const mi_op* ops, uint32_
         return set_error(MI_EINVAL, "ragged_run_noalloc: %u ops exceed the static scratch limit of %u ops", n_ops,
                          MI_RAGGED_NOALLOC_MAX_OPS);
     if (n_ops == 0) return MI_OK;
+    if (!aligned8(ops) || !aligned8(in) || !aligned8(out))
+        return set_error(MI_EINVAL, "ragged_run_noalloc: ops, in and out must be 8-byte aligned");
     int cur = -1;
     MI_CUDA_TRY(cudaGetDevice(&cur));
     if (cur != ctx->device) MI_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -774,6 +776,22 @@ extern "C" mi_status mi_ragged_run_noalloc(mi_ctx ctx, const mi_op* ops, uint32_
     MI_TRY(rg::noalloc_scratch(&scratch));
     return ragged_launch(ctx, ops, n_ops, in, out, carry_out, scratch, rg::Scratch::words(MI_RAGGED_NOALLOC_MAX_OPS) * 4,
                          ctx->ragged_ntt_min, reinterpret_cast<cudaStream_t>(stream));
+}
+
+// The skipped-op count of the last no-alloc run on the context's device, read
+// from the static array (the count that mi_ragged_invalid reads from a caller
+// scratch buffer).  Synchronous; allocates nothing.
+extern "C" mi_status mi_ragged_invalid_noalloc(mi_ctx ctx, uint32_t* count) {
+    using namespace mi;
+    if (ctx == nullptr || count == nullptr) return set_error(MI_EINVAL, "ragged_invalid_noalloc: null pointer");
+    int cur = -1;
+    MI_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != ctx->device) MI_CUDA_TRY(cudaSetDevice(ctx->device));
+    void* scratch = nullptr;
+    MI_TRY(rg::noalloc_scratch(&scratch));
+    MI_CUDA_TRY(cudaMemcpy(count, static_cast<const uint32_t*>(scratch) + rg::Scratch::INVALID, 4,
+                           cudaMemcpyDeviceToHost));
+    return MI_OK;
 }
 
 namespace mi {

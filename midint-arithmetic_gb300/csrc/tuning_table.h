@@ -1,5 +1,5 @@
 // tuning_table.h -- defaults of the tunable launch choices, written by
-// midint-arithmetic_gb300/autotune.py from measurements on NVIDIA GB300 (2026-12-03; the
+// midint-arithmetic_gb300/autotune.py from measurements on NVIDIA GB300 (2026-12-04; the
 // record of the run is midint-arithmetic_gb300/tuning.json).  Hand edits are
 // overwritten by the next tuning run.
 #pragma once
@@ -14,6 +14,9 @@ constexpr uint32_t kPlainNttMin = 160;
 // mi_mul_lo_u64: low halves of products of at least this many u64 limbs come
 // from the NTT kernel (2049 = never).
 constexpr uint32_t kLoNttMin = 320;
+// mi_poly_u64: composites of at least this many u64 limbs run their four
+// products on the NTT (2049 = never).
+constexpr uint32_t kPolyNttMin = 448;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257).
 constexpr uint32_t kRaggedNttMin = 96;

@@ -34,7 +34,8 @@ RAGGED_NOALLOC_MAX_OPS = 65536
 _P, _U32, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
 _S = ctypes.c_int  # mi_status
 (TUNE_PLAIN_NTT_MIN, TUNE_RAGGED_NTT_MIN, TUNE_ADD_THREAD_BYTES, TUNE_HOST_CHUNKS, TUNE_HOST_ZERO_COPY,
- TUNE_WIDE_SPIN_LIMIT, TUNE_WIDE_WITHHOLD, TUNE_WIDE_ROUND_TILES, TUNE_HOST_ZC_BLOCKS, TUNE_LO_NTT_MIN) = range(10)
+ TUNE_WIDE_SPIN_LIMIT, TUNE_WIDE_WITHHOLD, TUNE_WIDE_ROUND_TILES, TUNE_HOST_ZC_BLOCKS, TUNE_LO_NTT_MIN,
+ TUNE_POLY_NTT_MIN) = range(11)
 SIGNATURES = {
     "mi_version": (_I, []),
     "mi_status_string": (ctypes.c_char_p, [_I]),
@@ -68,10 +69,13 @@ SIGNATURES = {
     "mi_mul_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_compat_gpuMulFFT_u16": (_S, [_I, _U32, _P, _P, _P]),
     "mi_ntt_raw": (_S, [ctypes.c_uint64, ctypes.c_uint64, _U32, _U32, _I, _P, _P, _P]),
+    "mi_ntt32_raw": (_S, [_P, _U32, _U32, _I, _P, _P, _P]),
+    "mi_ntt32_prime": (_S, [_U32, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
     "mi_ragged_scratch_bytes": (_S, [_U32, ctypes.POINTER(ctypes.c_size_t)]),
     "mi_ragged_run": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "mi_ragged_invalid": (_S, [_P, ctypes.POINTER(_U32)]),
     "mi_ragged_run_noalloc": (_S, [_P, _P, _U32, _P, _P, _P, _P]),
+    "mi_ragged_invalid_noalloc": (_S, [_P, ctypes.POINTER(_U32)]),
     "mi_ragged_graph_create": (_S, [_P, _P, _U32, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)]),
     "mi_graph_launch": (_S, [_P, _P]),
     "mi_graph_destroy": (_S, [_P]),
@@ -248,6 +252,12 @@ class Context:
         check(load().mi_ragged_run_noalloc(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out), _ptr(carry),
                                            _ptr(stream)))
 
+    def ragged_invalid_noalloc(self) -> int:
+        """Ops the last no-alloc ragged run on this device skipped as invalid."""
+        v = ctypes.c_uint32()
+        check(load().mi_ragged_invalid_noalloc(self.handle, ctypes.byref(v)))
+        return v.value
+
     def ragged_graph(self, ops, n_ops: int, pool_in, pool_out, scratch, scratch_bytes: int, carry=None) -> "Graph":
         h = ctypes.c_void_p()
         check(load().mi_ragged_graph_create(self.handle, _ptr(ops), n_ops, _ptr(pool_in), _ptr(pool_out),
@@ -360,6 +370,24 @@ def ntt_raw(p: int, g: int, two_adicity: int, a: np.ndarray, b: np.ndarray | Non
     out = np.empty_like(a)
     bb = None if b is None else np.ascontiguousarray(b, dtype=np.uint64)
     check(load().mi_ntt_raw(p, g, two_adicity, a.size, 0 if b is None else 1, _ptr(a), _ptr(bb), _ptr(out)))
+    return out
+
+
+def ntt32_prime(q: int) -> tuple[int, int]:
+    """(p, g): production prime q (0..4) of the NTT multiplication kernels and
+    its primitive root."""
+    p, g = ctypes.c_uint32(), ctypes.c_uint32()
+    check(load().mi_ntt32_prime(q, ctypes.byref(p), ctypes.byref(g)))
+    return p.value, g.value
+
+
+def ntt32_raw(ctx: "Context", q: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:
+    """The multiplication kernels' transform on production prime q: forward
+    NTT of `a` (natural order) or, with `b`, the cyclic convolution mod p."""
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    out = np.empty_like(a)
+    bb = None if b is None else np.ascontiguousarray(b, dtype=np.uint32)
+    check(load().mi_ntt32_raw(ctx.handle, q, a.size, 0 if b is None else 1, _ptr(a), _ptr(bb), _ptr(out)))
     return out
 
 

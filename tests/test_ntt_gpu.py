@@ -125,3 +125,72 @@ def test_compat_gpuMulFFT(lib):
         got = rs.view(np.uint16)[: n * M].view(np.uint32)
         assert np.array_equal(got, g[f"mul_{m32}"])
         assert not rs[n * M // 2:].any()
+
+
+# --- the production transform (ntt32.cuh) on its own ---------------------------
+
+def _order_2s(p: int, g: int) -> tuple[int, int]:
+    """(g', s): g' = g^((p-1)/2^s) of order 2^s, s the 2-adicity of p - 1, so
+    the oracle's root for length L, g'^(2^s / L), is g^((p-1)/L)."""
+    s = ((p - 1) & -(p - 1)).bit_length() - 1
+    return pow(g, (p - 1) >> s, p), s
+
+
+@pytest.mark.parametrize("q", range(5))
+@pytest.mark.parametrize("length", [256, 512, 1024, 2048, 4096])
+def test_production_transform_matches_oracle(ctx, q, length):
+    p, g = midint.ntt32_prime(q)
+    g2, s = _order_2s(p, g)
+    rng = np.random.default_rng(1000 * q + length)
+    a = rng.integers(0, p, size=length, dtype=np.uint64)
+    b = rng.integers(0, p, size=length, dtype=np.uint64)
+    fwd = midint.ntt32_raw(ctx, q, a.astype(np.uint32))
+    assert np.array_equal(fwd.astype(np.uint64), O.ntt_forward(p, g2, s, a))
+    conv = midint.ntt32_raw(ctx, q, a.astype(np.uint32), b.astype(np.uint32))
+    assert np.array_equal(conv.astype(np.uint64), O.ntt_conv(p, g2, s, a, b))
+
+
+@pytest.mark.parametrize("q", [0, 4])
+@pytest.mark.parametrize("length", [256, 4096])
+def test_production_transform_edge_residues(ctx, q, length):
+    p, g = midint.ntt32_prime(q)
+    g2, s = _order_2s(p, g)
+    top = np.full(length, p - 1, np.uint64)              # the largest residues
+    delta = np.zeros(length, np.uint64)
+    delta[0] = 1
+    assert (midint.ntt32_raw(ctx, q, delta.astype(np.uint32)) == 1).all()   # spectrum of a unit impulse
+    assert np.array_equal(midint.ntt32_raw(ctx, q, top.astype(np.uint32)).astype(np.uint64),
+                          O.ntt_forward(p, g2, s, top))
+    assert np.array_equal(midint.ntt32_raw(ctx, q, top.astype(np.uint32), top.astype(np.uint32)).astype(np.uint64),
+                          O.ntt_conv(p, g2, s, top, top))
+    # inputs at or above p are reduced mod p first
+    big = np.full(length, 0xFFFFFFFF, np.uint64)
+    assert np.array_equal(midint.ntt32_raw(ctx, q, big.astype(np.uint32)).astype(np.uint64),
+                          O.ntt_forward(p, g2, s, big % p))
+
+
+def test_mul_ntt_rejects_misaligned_buffers(ctx, devmem):
+    # the transform kernels read 8-byte words: 4-byte aligned rows are refused
+    # on the host (the size-dispatched entry points take the classical kernel)
+    a, b = carry_stress(2, 300, seed=5)
+    ba, pa = devmem.put(a, 1)
+    bb, pb = devmem.put(b, 1)
+    br, pr = devmem.empty_words(4 * a.size, 1)
+    with pytest.raises(midint.MidintError) as e:
+        ctx.mul_ntt(pa, pb, pr, 2, 300, stream=_stream())
+    assert e.value.status == midint.MI_EINVAL
+
+
+@pytest.mark.parametrize("m", [200, 400, 2048])
+def test_size_dispatch_on_misaligned_rows_matches_oracle(ctx, devmem, m):
+    a, b = carry_stress(3, m, seed=m + 9)
+    ba, pa = devmem.put(a, 1)
+    bb, pb = devmem.put(b, 1)
+    br, pr = devmem.empty_words(4 * a.size, 1)
+    ctx.mul(pa, pb, pr, 3, m, stream=_stream())
+    torch.cuda.synchronize()
+    assert np.array_equal(devmem.get(br, 4 * a.size, 1), O.mul(a, b, m, True))
+    br2, pr2 = devmem.empty_words(2 * a.size, 1)
+    ctx.mul_lo(pa, pb, pr2, 3, m, stream=_stream())
+    torch.cuda.synchronize()
+    assert np.array_equal(devmem.get(br2, 2 * a.size, 1), O.mul(a, b, m, False))

@@ -125,6 +125,20 @@ def test_ragged_invalid_ops_are_skipped(ctx):
     oracle_check(ops, pool, out, carry, sample=[0, 1])
 
 
+def test_ragged_rejects_misaligned_pools(ctx):
+    ops, pool, out_limbs = W.ragged_ops(n_ops=10, seed=4)
+    d_ops = torch.from_numpy(ops.view(np.uint8).copy()).to("cuda:0")
+    d_in = torch.from_numpy(pool.view(np.int64)).to("cuda:0")
+    d_out = torch.zeros(out_limbs + 1, dtype=torch.int64, device="cuda:0")
+    sb = midint.ragged_scratch_bytes(ops.size)
+    scr = torch.empty(sb // 4 + 1, dtype=torch.int32, device="cuda:0")
+    with pytest.raises(midint.MidintError) as e:
+        ctx.ragged_run(d_ops, ops.size, d_in, d_out.data_ptr() + 4, scr, sb, stream=_stream())
+    assert e.value.status == midint.MI_EINVAL
+    with pytest.raises(midint.MidintError):
+        ctx.ragged_run_noalloc(d_ops, ops.size, d_in.data_ptr() + 4, d_out, stream=_stream())
+
+
 def test_ragged_graph_replay_matches_direct_run(ctx):
     ops, pool, out_limbs = W.ragged_ops(n_ops=5000, seed=11)
     direct, c1, _ = run_ragged(ctx, ops, pool, out_limbs)

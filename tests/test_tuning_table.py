@@ -24,6 +24,7 @@ def test_table_matches_record():
     picks = json.load(open(os.path.join(PKG, "tuning.json")))["picks"]
     assert table["kPlainNttMin"] == picks["plain_ntt_min"]
     assert table["kLoNttMin"] == picks["lo_ntt_min"]
+    assert table["kPolyNttMin"] == picks["poly_ntt_min"]
     assert table["kRaggedNttMin"] == picks["ragged_ntt_min"]
     assert table["kAddThreadBytes"] == picks["add_thread_bytes"]
     assert table["kHostChunks"] == picks["host_chunks"]
@@ -35,6 +36,7 @@ def test_picks_are_accepted_values():
     picks = json.load(open(os.path.join(PKG, "tuning.json")))["picks"]
     assert 1 <= picks["plain_ntt_min"] <= 2049
     assert 1 <= picks["lo_ntt_min"] <= 2049
+    assert 1 <= picks["poly_ntt_min"] <= 2049
     assert 1 <= picks["ragged_ntt_min"] <= 257
     assert len(picks["add_thread_bytes"]) == 13 and set(picks["add_thread_bytes"]) <= {16, 32, 64}
     assert all(1 <= c <= 64 for c in picks["host_chunks"])
@@ -69,6 +71,10 @@ def test_recorded_crossovers_follow_the_rule():
         faster = {m: rec[key][str(m)]["ntt_ns_per_product"] < rec[key][str(m)]["classical_ns_per_product"]
                   for m in sizes}
         assert crossover_pick(sizes, faster) == rec["picks"][pick], key
+    poly = rec["poly_crossover"]
+    sizes = sorted(int(m) for m in poly)
+    faster = {m: poly[str(m)]["ntt_ns_per_instance"] < poly[str(m)]["classical_ns_per_instance"] for m in sizes}
+    assert crossover_pick(sizes, faster) == rec["picks"]["poly_ntt_min"]
 
 
 def test_header_is_what_the_tuner_writes():

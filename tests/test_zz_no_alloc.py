@@ -58,6 +58,27 @@ def test_noalloc_matches_scratch_entry_point_on_two_calls_in_a_row(ctx):
         assert np.array_equal(got_c[adds], want_c[adds])
 
 
+def test_noalloc_at_its_static_limit(ctx):
+    # exactly as many ops as the static array is sized for
+    ops, pool, out_limbs = W.ragged_ops(n_ops=midint.RAGGED_NOALLOC_MAX_OPS, seed=23)
+    got_out, got_c = without_scratch(ctx, ops, pool, out_limbs)
+    assert ctx.ragged_invalid_noalloc() == 0
+    want_out, want_c = with_scratch(ctx, ops, pool, out_limbs)
+    assert np.array_equal(got_out, want_out)
+    adds = ops["kind"] == 0
+    assert np.array_equal(got_c[adds], want_c[adds])
+
+
+def test_noalloc_counts_invalid_ops(ctx):
+    # a bad kind, a zero length and an over-long operand are skipped and counted
+    ops, pool, out_limbs = W.pack_ops(np.array([0, 1, 1, 0, 7], np.uint32), np.array([3, 5, 0, 2000, 4], np.uint32),
+                                      np.array([3, 6, 4, 3, 4], np.uint32), 3)
+    got_out, got_c = without_scratch(ctx, ops, pool, out_limbs)
+    assert ctx.ragged_invalid_noalloc() == 3
+    want_out, want_c = with_scratch(ctx, ops, pool, out_limbs)
+    assert np.array_equal(got_out, want_out) and got_c[0] == want_c[0]
+
+
 def test_noalloc_refuses_lists_beyond_its_static_scratch(ctx):
     n = midint.RAGGED_NOALLOC_MAX_OPS + 1
     dummy = torch.zeros(8, dtype=torch.int64, device="cuda:0")
