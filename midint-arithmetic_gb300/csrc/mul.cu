@@ -3,10 +3,17 @@
 // Counterpart of the reference's bmulKerQ (cuda/ker-classic-mul.cu.h:468-498),
 // which returns the low half of the product of two m-limb operands.  Each
 // instance is one square product of mul_core.cuh, computed by a group of
-// NT = pow2ceil(n32/8) threads; a block of max(256, NT) threads holds 256/NT
-// groups and strides over the batch.  `full` selects the 2*n32-limb product or
-// its low n32 limbs (the reference's semantics); low halves of more than one
-// block of limbs go to the half-work kernel of mul_lo.cu.
+// NT = pow2ceil(n32/8) threads.  Groups of 16 or 32 threads run in blocks of
+// one warp, launched as one block per warp's worth of instances: the blocks
+// of an SM then start and finish at different times, so one warp's carry
+// resolution overlaps the others' tile loops, and the last wave spreads
+// evenly over the SMs (persistent blocks striding over the batch stay in phase
+// and measured 8-10 % slower; eight instances per 256-thread block 3 %
+// slower).  Other sizes, and launches capped at a few resident blocks per SM
+// (the zero-copy host path, whose cap was tuned on them), use blocks of
+// max(256, NT) threads that stride over the batch.  `full` selects the 2*n32-limb product or its low n32 limbs (the
+// reference's semantics); low halves of more than one block of limbs go to the
+// half-work kernel of mul_lo.cu.
 #include <cstdio>
 
 #include "common.cuh"
@@ -18,9 +25,11 @@ namespace {
 
 using classic::T;
 
-template <int NT>
+template <int NT, bool WB = false>
 struct MulShape {
-    static constexpr int BLOCK = NT > 256 ? NT : 256;
+    static constexpr bool WARP = WB && (NT == 16 || NT == 32);  // one-warp blocks
+    static constexpr int BLOCK = WARP ? 32 : (NT > 256 ? NT : 256);
+    static constexpr int MIN_BLOCKS = WARP ? 24 : (NT >= 512 ? 1 : (NT == 2 ? 2 : 3));
     static constexpr int IPB = BLOCK / NT;   // instances per block
     static constexpr int WPAD = NT * T;      // padded limbs per operand
     // operands (2 x IPB x WPAD words) + per-thread snapshot/combine words; the
@@ -28,11 +37,11 @@ struct MulShape {
     static constexpr size_t SMEM = size_t(2 * IPB * WPAD + BLOCK * classic::PER_T) * 4;
 };
 
-template <int NT, bool VEC>
-__global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 ? 2 : 3))
+template <int NT, bool VEC, bool WB>
+__global__ void __launch_bounds__(MulShape<NT, WB>::BLOCK, MulShape<NT, WB>::MIN_BLOCKS)
     k_mul(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ r, uint32_t n,
           uint32_t n32, bool full) {
-    using S = MulShape<NT>;
+    using S = MulShape<NT, WB>;
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* sA = smem;
     uint32_t* sB = sA + S::IPB * S::WPAD;
@@ -60,9 +69,11 @@ __global__ void __launch_bounds__(NT > 256 ? NT : 256, NT >= 512 ? 1 : (NT == 2 
         classic::stage_b<NT, VEC>(gB4, b + off, n32, valid, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
-        if (nb == NT)  // no padding: a compile-time trip count, unrolled in full for 8..32 steps
-            classic::square_product<NT, 1, (NT >= 8 && NT <= 32) ? NT : (NT >= 16 ? 8 : 2)>(gA, gB4, slots, scr, t,
-                                                                                         ulo, uhi, NT);
+        if (nb == NT)  // no padding: a compile-time trip count, unrolled in full for 8..32 steps; the
+                       // 32-thread groups in one-warp blocks prefetch each step's operands (the other
+                       // shapes would spill)
+            classic::square_product<NT, 1, (NT >= 8 && NT <= 32) ? NT : (NT >= 16 ? 8 : 2), NT == 32 && S::WARP>(
+                gA, gB4, slots, scr, t, ulo, uhi, NT);
         else
             classic::square_product<NT>(gA, gB4, slots, scr, t, ulo, uhi, nb);
         if (valid) {
@@ -90,19 +101,29 @@ mi_status capped_smem(size_t smem, uint32_t max_per_sm, size_t* out) {
     return MI_OK;
 }
 
-template <int NT, bool VEC>
-mi_status launch_nt(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
-                    cudaStream_t st, uint32_t max_per_sm) {
-    using S = MulShape<NT>;
-    auto kern = k_mul<NT, VEC>;
+template <int NT, bool VEC, bool WB>
+mi_status launch_shape(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
+                       cudaStream_t st, uint32_t max_per_sm) {
+    using S = MulShape<NT, WB>;
+    auto kern = k_mul<NT, VEC, WB>;
     size_t smem = S::SMEM;
     MI_TRY(capped_smem(S::SMEM, max_per_sm, &smem));
     MI_TRY(ensure_dyn_smem(kern, smem));
     uint64_t blocks = (uint64_t(n) + S::IPB - 1) / S::IPB;
-    const uint64_t cap = uint64_t(sm_count()) * 32;
+    // one block per unit of work for one-warp blocks (see above); the others
+    // stride over the batch from a grid of a few waves
+    const uint64_t cap = S::WARP ? (uint64_t(1) << 24) : uint64_t(sm_count()) * 32;
     if (blocks > cap) blocks = cap;
     MI_CUDA_TRY(launch_pdl(kern, dim3(uint32_t(blocks)), dim3(S::BLOCK), smem, st, a, b, r, n, n32, full));
     return MI_OK;
+}
+
+template <int NT, bool VEC>
+mi_status launch_nt(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t n, uint32_t n32, bool full,
+                    cudaStream_t st, uint32_t max_per_sm) {
+    if constexpr (NT == 16 || NT == 32)
+        if (max_per_sm == 0) return launch_shape<NT, VEC, true>(a, b, r, n, n32, full, st, 0);
+    return launch_shape<NT, VEC, false>(a, b, r, n, n32, full, st, max_per_sm);
 }
 
 template <bool VEC>

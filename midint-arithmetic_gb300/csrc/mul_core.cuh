@@ -158,7 +158,11 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 // Tile-loop unroll: deep for the plain kernels' wide groups (more loads in
 // flight per step), shallow where registers are short (small groups, the
 // ragged kernel's interleaved groups).
-template <int NT, int G = 1, int UNROLL = (NT >= 16 && G == 1) ? 8 : 2>
+//
+// PREFETCH: the operands of step k+1 are read from shared memory into
+// registers before the tile of step k is multiplied (16 more registers), so a
+// warp's multiply-adds never wait for its own loads.
+template <int NT, int G = 1, int UNROLL = (NT >= 16 && G == 1) ? 8 : 2, bool PREFETCH = false>
 __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
                                                uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                                uint32_t nb = NT) {
@@ -171,14 +175,33 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
 #pragma unroll
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
     const uint32_t snap_k = t < nb ? t : nb - 1;
+    uint4 na0, na1, nb0, nb1;  // step k+1's operands (PREFETCH)
+    if (PREFETCH) {
+        na0 = reinterpret_cast<const uint4*>(gA)[0];
+        na1 = reinterpret_cast<const uint4*>(gA)[1];
+        nb0 = gB4[t & uint32_t(NT - 1)];
+        nb1 = gB4[G * NT + (t & uint32_t(NT - 1))];
+    }
 #pragma unroll UNROLL
     for (uint32_t k = 0; k < nb; ++k) {
         const uint32_t j = (t - k) & uint32_t(NT - 1);
         uint32_t A[T], B[T];
-        const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * G * T)[0];
-        const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * G * T)[1];
-        const uint4 b0 = gB4[j];
-        const uint4 b1 = gB4[G * NT + j];
+        uint4 a0, a1, b0, b1;
+        if (PREFETCH) {
+            a0 = na0, a1 = na1, b0 = nb0, b1 = nb1;
+            if (k + 1 < nb) {
+                const uint32_t jn = (t - k - 1) & uint32_t(NT - 1);
+                na0 = reinterpret_cast<const uint4*>(gA + (k + 1) * G * T)[0];
+                na1 = reinterpret_cast<const uint4*>(gA + (k + 1) * G * T)[1];
+                nb0 = gB4[jn];
+                nb1 = gB4[G * NT + jn];
+            }
+        } else {
+            a0 = reinterpret_cast<const uint4*>(gA + k * G * T)[0];
+            a1 = reinterpret_cast<const uint4*>(gA + k * G * T)[1];
+            b0 = gB4[j];
+            b1 = gB4[G * NT + j];
+        }
         A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
         A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
         B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;

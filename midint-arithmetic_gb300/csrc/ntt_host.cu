@@ -104,8 +104,6 @@ mi_status ntt_tables_create(NttTables* T) {
         }
         P.kb[q][0] = shoup_pair(r32, p);
         P.kb[q][1] = shoup_pair(r64, p);
-        P.kone[q][0] = shoup_pair(1, p);
-        P.kone[q][1] = shoup_pair(r32, p);
     }
     int c = 0;
     for (int i = 1; i < 5; ++i)

@@ -87,8 +87,10 @@ __device__ __forceinline__ void lo_product(const uint64_t* x, const uint64_t* y,
     for (int q = 0; q < np; ++q) {
         const Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
         if constexpr (SQ) {
-            // X = F(x); pointwise X * (X * 2^32/L) / 2^32 = X^2 / L
-            const uint2 k0 = P.kone[q][0], k1 = P.kone[q][1], ks = P.ka_by_lg[q][LG - 8][1];
+            // X = F(x); pointwise X * (X * 2^32/L) / 2^32 = X^2 / L.  Conversion
+            // by 1: Shoup pairs of 1 (companion floor(2^32/p) = floor((2^32-1)/p),
+            // p odd) and of 2^32 mod p (b's pair kb[q][0])
+            const uint2 k0 = make_uint2(1u, 0xffffffffu / P.p[q]), k1 = P.kb[q][0], ks = P.ka_by_lg[q][LG - 8][1];
             uint32_t v[1][8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) v[0][j] = digit_residue<D48>(x, m, t + Pl::NT * j, f, k0, k1);
