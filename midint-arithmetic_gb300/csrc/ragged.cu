@@ -267,19 +267,22 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
     const uint32_t g = threadIdx.x / NT;
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     uint32_t* gsm = sm + g * ntt32::MulSmem<LG>::WORDS32;
-    if (g < tk.count) {
-        const mi_op op = P.ops[sorted[tk.first + g]];
-        ntt32::mul_one<LG, D48>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, P.out + op.r_off, op.la + op.lb,
-                                P.ntt, gsm, scr_warp);
-    } else {  // idle group: zero operands, no store, same barriers
-        ntt32::mul_one<LG, D48>(P.in, 0, P.in, 0, nullptr, 0, P.ntt, gsm, scr_warp);
-    }
+    // an idle group (g >= count) runs with zero operands, no store and the
+    // same barriers: one inlined product for both (two copies spilled)
+    const bool busy = g < tk.count;
+    mi_op op{};
+    if (busy) op = P.ops[sorted[tk.first + g]];
+    ntt32::mul_one<LG, D48>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, busy ? P.out + op.r_off : nullptr,
+                            op.la + op.lb, P.ntt, gsm, scr_warp);
 }
 
 // D48: the family of products with 48-bit digits on four primes (a kernel of
 // its own, so that neither digit mode's code raises the other's registers).
+// Two CTAs per SM at up to 128 registers: at three (85 registers) the 48-bit
+// products spilled 40-68 bytes at every transform length, and the list ran
+// 0.8 % slower (NTT band 0.896 against 0.878 ms on the 200000-op list).
 template <bool D48>
-__global__ void __launch_bounds__(256, 3) k_rg_ntt(Params P) {
+__global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
     constexpr int F = D48 ? 4 : 0;  // family
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the groups' shared memory
