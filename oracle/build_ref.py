@@ -4,8 +4,10 @@ Recipe: g++ on oracle/ref/ref_driver.cpp, which includes the reference's
 cuda/helper.h from the reference tree in place (never copied), against the
 GMP declaration shim oracle/ref/gmp.h and the installed libgmp.so.10; helper.h
 also names cudaGetErrorString, so libcudart is linked.  Outputs go only to
-oracle/_ref/.  Needs the reference tree; returns None when it is absent (the
-GPU machines have no copy of it and use the restatement in orc.c instead).
+oracle/_ref/.  Needs the reference tree: its cuda/ directory is
+$MIDINT_REFERENCE_CUDA when that is set, else the reference checkout this
+recipe was written against; returns None when neither exists (the GPU
+machines have no copy of it and use the restatement in orc.c instead).
 """
 from __future__ import annotations
 
@@ -13,7 +15,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_CUDA = "/root/reference/cuda"
+REF_CUDA = os.environ.get("MIDINT_REFERENCE_CUDA", "/root/reference/cuda")
 OUT_DIR = os.path.join(HERE, "_ref")
 OUT = os.path.join(OUT_DIR, "libref.so")
 CUDA = "/usr/local/cuda"
