@@ -676,7 +676,11 @@ def ntt_section(args, ctx, dev, stream, world, rank) -> dict:
         "roofline": {"bound": "int-mul", "achieved": achieved / 1e9, "peak": peak / 1e9,
                      "unit": "G 32x32-bit partial products/s", "frac": achieved / peak,
                      "per_unit": f"{mults} 32x32-bit integer multiplies per instance (five 30-bit primes)",
-                     "peak_source": "mi_calib_mul32_peak (measured in-process)"},
+                     "peak_source": "mi_calib_mul32_peak (measured in-process)",
+                     # the canonical schedule (3 primes near 2^62, 64-bit digits, L = 2048: 107520
+                     # 64-bit modular multiplies per instance, 12 32x32-bit products each) over the same
+                     # time and ceiling: above 1 when the schedule run here needs fewer multiplies
+                     "canonical_equivalent_frac": n_ntt * 107520 * 12 / (ms * 1e-3) / peak},
         "l2": f"{sets} rotating sets of {set_bytes >> 20} MiB",
     }
     del da, db, dr
