@@ -27,8 +27,10 @@
 // completes (one predicated store sequence per step); the second is the final
 // accumulator minus the snapshot.  Every output block of T limbs is then
 // L_s + H_(s-1) + O_(s-2) (low, high and overflow words of the anti-diagonal
-// values), added with two carry-lookahead passes over the group
-// (mi::group_carry) -- the reference's low/high/carry publish and baddRegs.
+// values): each block's three-way sum hands its carry of 0..2 to the next
+// block, and one carry-lookahead pass over the group (mi::group_carry)
+// resolves the one-bit ripple that remains (combine_blocks) -- the
+// reference's low/high/carry publish and baddRegs.
 #pragma once
 
 #include "common.cuh"
@@ -96,6 +98,80 @@ __device__ __forceinline__ void fold(const uint32_t* a, const uint32_t* b, const
 #pragma unroll
     for (int c = 1; c < T; ++c) addc_cc(f[T + c], cc[c]);
     addc(f[2 * T], cc[T]);
+}
+
+// r = x + y + o (o at word 0) as T words; returns the carry out, 0..2.
+__device__ __forceinline__ uint32_t add3_block(const uint32_t (&x)[T], const uint32_t (&y)[T], uint32_t o,
+                                               uint32_t (&r)[T]) {
+#pragma unroll
+    for (int w = 0; w < T; ++w) r[w] = x[w];
+    uint32_t k = 0;
+    add_cc(r[0], y[0]);
+#pragma unroll
+    for (int w = 1; w < T; ++w) addc_cc(r[w], y[w]);
+    addc(k, 0u);
+    add_cc(r[0], o);
+#pragma unroll
+    for (int w = 1; w < T; ++w) addc_cc(r[w], 0u);
+    addc(k, 0u);
+    return k;
+}
+
+// r += c (a word at word 0) with the carry through the block; returns the
+// carry out (0 or 1).
+__device__ __forceinline__ uint32_t add_word_block(uint32_t (&r)[T], uint32_t c) {
+    uint32_t e = 0;
+    add_cc(r[0], c);
+#pragma unroll
+    for (int w = 1; w < T; ++w) addc_cc(r[w], 0u);
+    addc(e, 0u);
+    return e;
+}
+
+__device__ __forceinline__ bool all_ones(const uint32_t (&r)[T]) {
+    uint32_t a = r[0];
+#pragma unroll
+    for (int w = 1; w < T; ++w) a &= r[w];
+    return a == MI_FULL_MASK;
+}
+
+// The group's 2NT output blocks in order, block q = t (lo) and q = NT + t
+// (hi) of thread t, each L_q + H_(q-1) + O_(q-2), carried through; the carry
+// out of the last block is dropped.  One pass: each block's three-way sum
+// leaves a carry of 0..2, handed to the next block's thread (a shuffle within
+// a warp; pair 18 of the shared slots, free by then, for wider groups) and
+// added there; what remains is a one-bit ripple, resolved with one
+// carry-lookahead pass per half.  `slots` is the group's pair array as in
+// square_product (pair w of thread l at slots[w*NT*G + l]).
+template <int NT, int G = 1>
+__device__ __forceinline__ void combine_blocks(const uint32_t (&Llo)[T], const uint32_t (&Hlo)[T], uint32_t Olo,
+                                               const uint32_t (&Lhi)[T], const uint32_t (&Hhi)[T], uint32_t Ohi,
+                                               uint2* slots, uint32_t* scr, uint32_t t, uint32_t (&ulo)[T],
+                                               uint32_t (&uhi)[T]) {
+    const uint32_t clo = add3_block(Llo, Hlo, Olo, ulo);
+    const uint32_t chi = add3_block(Lhi, Hhi, Ohi, uhi);
+    uint32_t in_lo, in_hi;  // carries of the preceding blocks (lane NT-1's lo block precedes lane 0's hi)
+    if constexpr (NT <= 32) {
+        const uint32_t mask = group_lanes<NT>();
+        const uint32_t plo = __shfl_up_sync(mask, clo, 1, NT);
+        const uint32_t phi = __shfl_up_sync(mask, chi, 1, NT);
+        const uint32_t top = __shfl_sync(mask, clo, NT - 1, NT);
+        in_lo = t ? plo : 0u;
+        in_hi = t ? phi : top;
+    } else {
+        slots[18 * NT * G + t] = make_uint2(clo, chi);
+        group_sync<NT>();
+        const uint2 prev = slots[18 * NT * G + (t ? t - 1 : NT - 1)];
+        in_lo = t ? prev.x : 0u;
+        in_hi = t ? prev.y : prev.x;
+    }
+    const uint32_t elo = add_word_block(ulo, in_lo);
+    const uint32_t ehi = add_word_block(uhi, in_hi);
+    uint32_t c0, c1;
+    const uint32_t rlo = group_carry<NT>(elo != 0, all_ones(ulo), 0u, &c0, scr);
+    const uint32_t rhi = group_carry<NT>(ehi != 0, all_ones(uhi), c0, &c1, scr);
+    add_word_block(ulo, rlo);
+    add_word_block(uhi, rhi);
 }
 
 // Stages `n32` limbs of an operand row into the group's A area (blocks of T
@@ -270,40 +346,7 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         Llo[w] = d1[w];
         Lhi[w] = d2[w];
     }
-    {
-        bool g0, p0, g1, p1;
-        uint32_t c0, c1;
-        chunk_add<uint32_t, T>(Llo, Hlo, ulo, g0, p0);
-        chunk_add<uint32_t, T>(Lhi, Hhi, uhi, g1, p1);
-        const uint32_t cl = group_carry<NT>(g0, p0, 0u, &c0, scr);
-        const uint32_t ch = group_carry<NT>(g1, p1, c0, &c1, scr);
-        chunk_inc<uint32_t, T>(ulo, cl);
-        chunk_inc<uint32_t, T>(uhi, ch);
-    }
-    {
-        uint32_t Zlo[T], Zhi[T];
-#pragma unroll
-        for (int w = 0; w < T; ++w) {
-            Zlo[w] = 0;
-            Zhi[w] = 0;
-        }
-        Zlo[0] = Olo;
-        Zhi[0] = Ohi;
-        uint32_t vlo[T], vhi[T];
-        bool g0, p0, g1, p1;
-        uint32_t c0, c1;
-        chunk_add<uint32_t, T>(ulo, Zlo, vlo, g0, p0);
-        chunk_add<uint32_t, T>(uhi, Zhi, vhi, g1, p1);
-        const uint32_t cl = group_carry<NT>(g0, p0, 0u, &c0, scr);
-        const uint32_t ch = group_carry<NT>(g1, p1, c0, &c1, scr);
-        chunk_inc<uint32_t, T>(vlo, cl);
-        chunk_inc<uint32_t, T>(vhi, ch);
-#pragma unroll
-        for (int w = 0; w < T; ++w) {
-            ulo[w] = vlo[w];
-            uhi[w] = vhi[w];
-        }
-    }
+    combine_blocks<NT, G>(Llo, Hlo, Olo, Lhi, Hhi, Ohi, slots, scr, t, ulo, uhi);
 }
 
 // Stages `n32` limbs of an operand row in the two-plane layout of NB blocks
@@ -429,40 +472,7 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
     }
     const uint32_t Olo = (t >= 2) ? diag(t - 2, 2 * T) : 0u;
     const uint32_t Ohi = (qh >= 2) ? diag(qh - 2, 2 * T) : 0u;
-    {
-        bool g0, p0, g1, p1;
-        uint32_t c0, c1;
-        chunk_add<uint32_t, T>(Llo, Hlo, ulo, g0, p0);
-        chunk_add<uint32_t, T>(Lhi, Hhi, uhi, g1, p1);
-        const uint32_t cl = group_carry<NH>(g0, p0, 0u, &c0, scr);
-        const uint32_t ch = group_carry<NH>(g1, p1, c0, &c1, scr);
-        chunk_inc<uint32_t, T>(ulo, cl);
-        chunk_inc<uint32_t, T>(uhi, ch);
-    }
-    {
-        uint32_t Zlo[T], Zhi[T];
-#pragma unroll
-        for (int w = 0; w < T; ++w) {
-            Zlo[w] = 0;
-            Zhi[w] = 0;
-        }
-        Zlo[0] = Olo;
-        Zhi[0] = Ohi;
-        uint32_t vlo[T], vhi[T];
-        bool g0, p0, g1, p1;
-        uint32_t c0, c1;
-        chunk_add<uint32_t, T>(ulo, Zlo, vlo, g0, p0);
-        chunk_add<uint32_t, T>(uhi, Zhi, vhi, g1, p1);
-        const uint32_t cl = group_carry<NH>(g0, p0, 0u, &c0, scr);
-        const uint32_t ch = group_carry<NH>(g1, p1, c0, &c1, scr);
-        chunk_inc<uint32_t, T>(vlo, cl);
-        chunk_inc<uint32_t, T>(vhi, ch);
-#pragma unroll
-        for (int w = 0; w < T; ++w) {
-            ulo[w] = vlo[w];
-            uhi[w] = vhi[w];
-        }
-    }
+    combine_blocks<NH>(Llo, Hlo, Olo, Lhi, Hhi, Ohi, slots, scr, t, ulo, uhi);
 }
 
 // Stores the T limbs of `v` at limb o of a result row, clipped to rlen.
