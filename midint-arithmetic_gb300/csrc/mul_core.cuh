@@ -312,7 +312,30 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
 #pragma unroll
         for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
         subc(d2[ACC - 1], d1[ACC - 1]);
-        // D1 words 0..16 in pairs 0..8, D2 words in pairs 9..17
+    }
+
+    // output blocks s=t (lo) and s=t+NT (hi): L_s + H_(s-1) + O_(s-2).  The
+    // high and overflow words come from thread t-1 (t-2): its D1 for the lo
+    // block, its D2 for the hi block, where thread 0 (and 1 for O) wraps to
+    // the D1 of threads NT-1 (NT-2)
+    uint32_t Hlo[T], Hhi[T], Olo = 0, Ohi = 0;
+    if constexpr (NT <= 32) {
+        // within a warp: shuffles, each sender offering what its receiver needs
+        const uint32_t mask = group_lanes<NT>();
+        const uint32_t src1 = (t - 1) & uint32_t(NT - 1), src2 = (t - 2) & uint32_t(NT - 1);
+#pragma unroll
+        for (int w = 0; w < T; ++w) {
+            const uint32_t a = __shfl_sync(mask, d1[T + w], src1, NT);
+            const uint32_t b = __shfl_sync(mask, (t == NT - 1) ? d1[T + w] : d2[T + w], src1, NT);
+            Hlo[w] = t >= 1 ? a : 0u;
+            Hhi[w] = b;
+        }
+        const uint32_t o1 = __shfl_sync(mask, d1[2 * T], src2, NT);
+        const uint32_t o2 = __shfl_sync(mask, (t + 2 >= NT) ? d1[2 * T] : d2[2 * T], src2, NT);
+        Olo = t >= 2 ? o1 : 0u;
+        if constexpr (NT >= 2) Ohi = o2;
+    } else {
+        // across warps: D1 words 0..16 in pairs 0..8, D2 words in pairs 9..17
 #pragma unroll
         for (int w = 0; w < ACC / 2; ++w) {
             slot(w, t) = make_uint2(d1[2 * w], d1[2 * w + 1]);
@@ -320,25 +343,22 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         }
         slot(ACC / 2, t) = make_uint2(d1[ACC - 1], 0u);
         slot(9 + ACC / 2, t) = make_uint2(d2[ACC - 1], 0u);
-    }
-    group_sync<NT>();
-
-    // output blocks s=t (lo) and s=t+NT (hi): L_s + H_(s-1) + O_(s-2)
-    auto peer = [&](uint32_t lane, int which, int w) -> uint32_t {
-        const uint2 v = slot(which * 9 + w / 2, lane);
-        return (w & 1) ? v.y : v.x;
-    };
-    uint32_t Hlo[T], Hhi[T], Olo = 0, Ohi = 0;
+        group_sync<NT>();
+        auto peer = [&](uint32_t lane, int which, int w) -> uint32_t {
+            const uint2 v = slot(which * 9 + w / 2, lane);
+            return (w & 1) ? v.y : v.x;
+        };
 #pragma unroll
-    for (int w = 0; w < T; ++w) {
-        Hlo[w] = (t >= 1) ? peer(t - 1, 0, T + w) : 0u;
-        Hhi[w] = (t >= 1) ? peer(t - 1, 1, T + w) : peer(NT - 1, 0, T + w);
-    }
-    if (t >= 2) {
-        Olo = peer(t - 2, 0, 2 * T);
-        Ohi = peer(t - 2, 1, 2 * T);
-    } else {
-        if constexpr (NT >= 2) Ohi = (t == 1) ? peer(NT - 1, 0, 2 * T) : peer(NT - 2, 0, 2 * T);
+        for (int w = 0; w < T; ++w) {
+            Hlo[w] = (t >= 1) ? peer(t - 1, 0, T + w) : 0u;
+            Hhi[w] = (t >= 1) ? peer(t - 1, 1, T + w) : peer(NT - 1, 0, T + w);
+        }
+        if (t >= 2) {
+            Olo = peer(t - 2, 0, 2 * T);
+            Ohi = peer(t - 2, 1, 2 * T);
+        } else {
+            Ohi = (t == 1) ? peer(NT - 1, 0, 2 * T) : peer(NT - 2, 0, 2 * T);
+        }
     }
     uint32_t Llo[T], Lhi[T];
 #pragma unroll
