@@ -100,9 +100,10 @@ __device__ __forceinline__ void fold(const uint32_t* a, const uint32_t* b, const
     addc(f[2 * T], cc[T]);
 }
 
-// r = x + y + o (o at word 0) as T words; returns the carry out, 0..2.
+// r = x + y (+ z when given) + o (o at word 0) as T words; returns the carry
+// out, 0..2 (0..3 with z).
 __device__ __forceinline__ uint32_t add3_block(const uint32_t (&x)[T], const uint32_t (&y)[T], uint32_t o,
-                                               uint32_t (&r)[T]) {
+                                               uint32_t (&r)[T], const uint32_t* z = nullptr) {
 #pragma unroll
     for (int w = 0; w < T; ++w) r[w] = x[w];
     uint32_t k = 0;
@@ -110,6 +111,12 @@ __device__ __forceinline__ uint32_t add3_block(const uint32_t (&x)[T], const uin
 #pragma unroll
     for (int w = 1; w < T; ++w) addc_cc(r[w], y[w]);
     addc(k, 0u);
+    if (z != nullptr) {
+        add_cc(r[0], z[0]);
+#pragma unroll
+        for (int w = 1; w < T; ++w) addc_cc(r[w], z[w]);
+        addc(k, 0u);
+    }
     add_cc(r[0], o);
 #pragma unroll
     for (int w = 1; w < T; ++w) addc_cc(r[w], 0u);
@@ -142,13 +149,15 @@ __device__ __forceinline__ bool all_ones(const uint32_t (&r)[T]) {
 // a warp; pair 18 of the shared slots, free by then, for wider groups) and
 // added there; what remains is a one-bit ripple, resolved with one
 // carry-lookahead pass per half.  `slots` is the group's pair array as in
-// square_product (pair w of thread l at slots[w*NT*G + l]).
+// square_product (pair w of thread l at slots[w*NT*G + l]).  `alo`, when
+// given, is one more T-word addend of the thread's lo block (the sum of the
+// 2NT blocks must fit them: the carry out of the last block is dropped).
 template <int NT, int G = 1>
 __device__ __forceinline__ void combine_blocks(const uint32_t (&Llo)[T], const uint32_t (&Hlo)[T], uint32_t Olo,
                                                const uint32_t (&Lhi)[T], const uint32_t (&Hhi)[T], uint32_t Ohi,
                                                uint2* slots, uint32_t* scr, uint32_t t, uint32_t (&ulo)[T],
-                                               uint32_t (&uhi)[T]) {
-    const uint32_t clo = add3_block(Llo, Hlo, Olo, ulo);
+                                               uint32_t (&uhi)[T], const uint32_t* alo = nullptr) {
+    const uint32_t clo = add3_block(Llo, Hlo, Olo, ulo, alo);
     const uint32_t chi = add3_block(Lhi, Hhi, Ohi, uhi);
     uint32_t in_lo, in_hi;  // carries of the preceding blocks (lane NT-1's lo block precedes lane 0's hi)
     if constexpr (NT <= 32) {
@@ -238,10 +247,13 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 // PREFETCH: the operands of step k+1 are read from shared memory into
 // registers before the tile of step k is multiplied (16 more registers), so a
 // warp's multiply-adds never wait for its own loads.
+//
+// alo: when given, T more words added to the thread's output block t (lo)
+// in the same carry pass (the ragged products' pending window).
 template <int NT, int G = 1, int UNROLL = (NT >= 16 && G == 1) ? 8 : 2, bool PREFETCH = false>
 __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* gB4, uint2* slots, uint32_t* scr,
                                                uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
-                                               uint32_t nb = NT) {
+                                               uint32_t nb = NT, const uint32_t* alo = nullptr) {
     auto slot = [&](int w, uint32_t lane) -> uint2& { return slots[w * NT * G + lane]; };
     DiagAcc s;
 #pragma unroll
@@ -366,7 +378,7 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         Llo[w] = d1[w];
         Lhi[w] = d2[w];
     }
-    combine_blocks<NT, G>(Llo, Hlo, Olo, Lhi, Hhi, Ohi, slots, scr, t, ulo, uhi);
+    combine_blocks<NT, G>(Llo, Hlo, Olo, Lhi, Hhi, Ohi, slots, scr, t, ulo, uhi, alo);
 }
 
 // Stages `n32` limbs of an operand row in the two-plane layout of NB blocks

@@ -378,26 +378,14 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
         }
         if (c + 1 < chunks) load_chunk_regs<NT>(nxt, x, nx, (c + 1) * W, t);
         group_sync<NT>();
+        // the chunk's product plus the pending window, carried in one pass:
+        // the low half (limbs [cW, (c+1)W)) is final and the high half becomes
+        // the next window (the sum fits the 2W limbs: no carry out)
         uint32_t ulo[T], uhi[T];
-        classic::square_product<NT, G>(gA, gB4, slots, scr, t, ulo, uhi, valid ? (nby ? nby : 1u) : 1u);
-        // limbs [cW, (c+1)W) are final: the low half plus the pending window
-        uint32_t fin[T];
-        bool g0, p0;
-        uint32_t gc;
-        chunk_add<uint32_t, T>(ulo, pend, fin, g0, p0);
-        const uint32_t cin = group_carry<NT>(g0, p0, 0u, &gc, scr);
-        chunk_inc<uint32_t, T>(fin, cin);
-        if (valid) classic::store_pairs(rr, c * W + t * T, rlen, fin);
-        // the high half plus that carry becomes the next window (cannot overflow)
-        uint32_t z[T];
+        classic::square_product<NT, G>(gA, gB4, slots, scr, t, ulo, uhi, valid ? (nby ? nby : 1u) : 1u, pend);
+        if (valid) classic::store_pairs(rr, c * W + t * T, rlen, ulo);
 #pragma unroll
-        for (int w = 0; w < T; ++w) z[w] = 0;
-        z[0] = (t == 0) ? gc : 0u;
-        bool g1, p1;
-        uint32_t gc1;
-        chunk_add<uint32_t, T>(uhi, z, pend, g1, p1);
-        const uint32_t cin1 = group_carry<NT>(g1, p1, 0u, &gc1, scr);
-        chunk_inc<uint32_t, T>(pend, cin1);
+        for (int w = 0; w < T; ++w) pend[w] = uhi[w];
         group_sync<NT>();  // gA and the slots are reused by the next chunk
     }
     if (valid) classic::store_pairs(rr, chunks * W + t * T, rlen, pend);
