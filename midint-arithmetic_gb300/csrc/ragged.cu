@@ -17,14 +17,15 @@
 //       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh),
 //       one family with 64-bit digits on five primes and one with 48-bit
 //       digits on four for the products whose 48-bit digits fit the same L;
-//     * classical products with a shorter operand of up to 128 limbs, a task
-//       per warp: comb products when it has at most 8 limbs (each thread
-//       multiplies 16 words of the longer operand by all of it in registers),
-//       otherwise 32/NT products whose shorter operand fits NT tiles of 8 u32
+//     * classical products with a shorter operand of 9 to 128 limbs, a task
+//       per warp: 32/NT products whose shorter operand fits NT tiles of 8 u32
 //       limbs, broadcast to the group, while the longer one streams through
 //       in chunks of NT tiles, each chunk a square product (mul_core.cuh)
-//       added into a sliding window whose low half is final -- no padding of
-//       either operand to a power of two;
+//       whose carry pass also adds the pending window of the chunk before,
+//       the low half final -- no padding of either operand to a power of two;
+//     * comb products, shorter operand of at most 8 limbs, a family and a
+//       kernel of their own (each thread multiplies 16 words of the longer
+//       operand by all of the shorter one in registers);
 //     * the same chunked products for 129..256 limbs in 64-thread groups;
 //     * additions, a task per warp: lanes of one limb for additions of up to
 //       32 limbs, rows of 32 limbs per warp above that.
@@ -52,12 +53,12 @@ constexpr int K_CLS = 13;        // NT = 1..16 (one chunk), NT = 32 x chunks = 1
 constexpr int K_ADD = 11;        // GS = 1..32 lanes of one limb; one warp over 2..32 rows of 32 limbs
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
 constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
-constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_CMB = KEY_CLS + K_CLS, KEY_ADD = KEY_CMB + K_CMB,
-              KEY_C64 = KEY_ADD + K_ADD, KEY_N48 = KEY_C64 + K_C64;
-constexpr int K = KEY_N48 + K_N48;
-// families: NTT (64-bit digits), classical in a warp, additions, classical in
-// 64 threads, NTT with 48-bit digits
-constexpr int NFAM = 5;
+constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = KEY_CLS + K_CLS, KEY_C64 = KEY_ADD + K_ADD,
+              KEY_N48 = KEY_C64 + K_C64, KEY_CMB = KEY_N48 + K_N48;
+constexpr int K = KEY_CMB + K_CMB;
+// families: NTT (64-bit digits), classical square products in a warp,
+// additions, classical in 64 threads, NTT with 48-bit digits, comb products
+constexpr int NFAM = 6;
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
@@ -129,15 +130,17 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
     if (key < KEY_CLS) return 2048u >> (8 + key - KEY_NTT);          // NTT: 256 threads / (L/8)
-    if (key >= KEY_N48) return 2048u >> (8 + key - KEY_N48);
-    if (key < KEY_CMB) {                                              // classical: one warp
+    if (key < KEY_ADD) {                                              // classical: one warp
         const uint32_t k = key - KEY_CLS;
         return k < 5 ? 32u >> k : 1u;
     }
-    if (key < KEY_ADD) return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;  // comb: 32 / group
-    if (key >= KEY_C64) return 4u;                                    // classical: 256 threads / 64
-    const uint32_t k = key - KEY_ADD;                                 // add: one warp
-    return k < 6 ? 32u >> k : kAddRowOps;
+    if (key < KEY_C64) {                                              // add: one warp
+        const uint32_t k = key - KEY_ADD;
+        return k < 6 ? 32u >> k : kAddRowOps;
+    }
+    if (key < KEY_N48) return 4u;                                     // classical: 256 threads / 64
+    if (key < KEY_CMB) return 2048u >> (8 + key - KEY_N48);          // NTT, 48-bit digits
+    return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;           // comb: 32 / group
 }
 
 // Binning.  Blocks of classify and scatter own the same contiguous ranges of
@@ -165,11 +168,13 @@ __global__ void __launch_bounds__(256) k_classify(const mi_op* __restrict__ ops,
 
 // First key of family f (f = NFAM: the end of the key space).
 __host__ __device__ constexpr int fam_base(int f) {
-    return f == 0 ? KEY_NTT : (f == 1 ? KEY_CLS : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : (f == 4 ? KEY_N48 : K))));
+    return f == 0 ? KEY_NTT
+                  : (f == 1 ? KEY_CLS
+                            : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : (f == 4 ? KEY_N48 : (f == 5 ? KEY_CMB : K)))));
 }
 static_assert(fam_base(1) - fam_base(0) <= 32 && fam_base(2) - fam_base(1) <= 32 &&
                   fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32 &&
-                  fam_base(5) - fam_base(4) <= 32,
+                  fam_base(5) - fam_base(4) <= 32 && fam_base(6) - fam_base(5) <= 32,
               "a family's keys fit one warp");
 
 // One warp per family scans its keys in c_order (shuffle scans): op offsets
@@ -494,15 +499,6 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
         t = __shfl_sync(MI_FULL_MASK, t, 0);
         if (t >= ntasks) break;
         const Task tk = decode(P.scr, 1, t);
-        if (tk.key >= uint32_t(KEY_CMB)) {
-            const uint32_t ki = tk.key - KEY_CMB;
-            if (ki == 0) comb_task<4>(P, tk);
-            else if (ki == 1) comb_task<8>(P, tk);
-            else if (ki == 2) comb_task<16>(P, tk);
-            else comb_task<32>(P, tk);
-            __syncwarp();
-            continue;
-        }
         switch (min(tk.key - KEY_CLS, 5u)) {
             case 0: classic_task<1>(P, tk, wsm, nullptr); break;
             case 1: classic_task<2>(P, tk, wsm, nullptr); break;
@@ -511,6 +507,29 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
             case 4: classic_task<16>(P, tk, wsm, nullptr); break;
             default: classic_task<32>(P, tk, wsm, nullptr); break;
         }
+        __syncwarp();
+    }
+    pdl_wait();  // complete only after the task kernel launched before it
+}
+
+// Comb products (shorter operand of at most 8 limbs): a family and a kernel
+// of their own, so that neither these nor the square products carry the
+// other's code and registers.
+__global__ void __launch_bounds__(256, 2) k_rg_comb(Params P) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 5];
+    pdl_trigger();
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 5, 1u);
+        t = __shfl_sync(MI_FULL_MASK, t, 0);
+        if (t >= ntasks) break;
+        const Task tk = decode(P.scr, 5, t);
+        const uint32_t ki = tk.key - KEY_CMB;
+        if (ki == 0) comb_task<4>(P, tk);
+        else if (ki == 1) comb_task<8>(P, tk);
+        else if (ki == 2) comb_task<16>(P, tk);
+        else comb_task<32>(P, tk);
         __syncwarp();
     }
     pdl_wait();  // complete only after the task kernel launched before it
@@ -647,7 +666,7 @@ mi_status init_device() {
     // classical keys by descending cost: 32-thread groups from 8 chunks down
     // to 1, then groups of 16, 8, 4, 2, 1 threads (one chunk each)
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + (K_CLS - 1 - k));
-    // comb keys after them, the most passes first
+    // the comb family, the most passes first
     const int comb[K_CMB] = {6, 5, 4, 3, 2, 1, 0};
     for (int k = 0; k < K_CMB; ++k) order[KEY_CMB + k] = uint16_t(KEY_CMB + comb[k]);
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
@@ -707,6 +726,7 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
     if (P.ntt_min > 129)
         MI_CUDA_TRY(launch_pdl(k_rg_c64, persistent_grid((const void*)k_rg_c64, kC64Smem), 256, kC64Smem, st, P));
+    MI_CUDA_TRY(launch_pdl(k_rg_comb, persistent_grid((const void*)k_rg_comb, 0), 256, 0, st, P));
     MI_CUDA_TRY(launch_pdl(k_rg_add, persistent_grid((const void*)k_rg_add, 0), 256, 0, st, P));
     return MI_OK;
 }
