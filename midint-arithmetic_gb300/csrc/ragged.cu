@@ -239,28 +239,51 @@ __global__ void __launch_bounds__(256) k_scatter(uint32_t n, uint32_t* __restric
     }
 }
 
-// Task t of family f -> (key, index of its first op in `sorted`, op count).
+// Task t of a family -> (key, index of its first op in `sorted`, op count).
 struct Task {
     uint32_t key, first, count;
 };
 
-__device__ __forceinline__ Task decode(const uint32_t* scr, int f, uint32_t t) {
-    const int base = fam_base(f);
-    const int nk = fam_base(f + 1) - base;
-    const uint32_t* ts = scr + Scratch::TS + f + base;  // nk + 1 monotone starts
-    int lo = 0, hi = nk;                                // ts[lo] <= t < ts[hi]
+// A family's decode table in shared memory, loaded once per block from the
+// scratch: the task start of every order position of its keys (and the
+// sentinel), and each position's key, op offset and op count, so that
+// decoding a task is a binary search in shared memory rather than a chain of
+// dependent global loads.
+struct FamTab {
+    uint32_t ts[33];
+    uint32_t key[32], first[32], count[32];
+};
+
+// By every thread of the block; a __syncthreads must follow before use.
+__device__ __forceinline__ void load_tab(FamTab& tab, const uint32_t* scr, int f) {
+    const int base = fam_base(f), nk = fam_base(f + 1) - base;
+    for (int i = threadIdx.x; i <= nk; i += blockDim.x) {
+        tab.ts[i] = scr[Scratch::TS + f + base + i];
+        if (i < nk) {
+            const uint32_t key = c_order[base + i];
+            tab.key[i] = key;
+            tab.first[i] = scr[Scratch::OPOFF + key];
+            tab.count[i] = scr[Scratch::COUNTS + key];
+        }
+    }
+}
+
+// Task t of family F from its table.
+template <int F>
+__device__ __forceinline__ Task decode_tab(const FamTab& tab, uint32_t t) {
+    constexpr int nk = fam_base(F + 1) - fam_base(F);
+    int lo = 0, hi = nk;  // ts[lo] <= t < ts[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (ts[mid] <= t) lo = mid; else hi = mid;
+        if (tab.ts[mid] <= t) lo = mid; else hi = mid;
     }
-    const uint32_t key = c_order[base + lo];
+    const uint32_t key = tab.key[lo];
     const uint32_t opt = ops_per_task(key);
-    const uint32_t local = t - ts[lo];
-    const uint32_t cnt = scr[Scratch::COUNTS + key];
+    const uint32_t local = t - tab.ts[lo];
     Task T;
     T.key = key;
-    T.first = scr[Scratch::OPOFF + key] + local * opt;
-    T.count = min(opt, cnt - local * opt);
+    T.first = tab.first[lo] + local * opt;
+    T.count = min(opt, tab.count[lo] - local * opt);
     return T;
 }
 
@@ -292,15 +315,17 @@ __global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the groups' shared memory
     __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
+    __shared__ FamTab tab;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + F];
     pdl_trigger();  // the next family's kernel may start as this one's blocks finish
+    load_tab(tab, P.scr, F);
     if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + F, 1u);
     __syncthreads();
     for (uint32_t it = 0;; ++it) {
         const uint32_t t = s_task[it & 1];
         if (t >= ntasks) break;
         if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + F, 1u);
-        const Task tk = decode(P.scr, F, t);
+        const Task tk = decode_tab<F>(tab, t);
         switch (tk.key - (D48 ? KEY_N48 : KEY_NTT)) {
             case 0: ntt_task<8, D48>(P, tk, smem, scr_warp); break;
             case 1: ntt_task<9, D48>(P, tk, smem, scr_warp); break;
@@ -491,14 +516,19 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
     extern __shared__ __align__(16) uint32_t smem32[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     uint32_t* wsm = smem32 + warp * CLS_WARP_WORDS;
+    __shared__ FamTab tab;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 1];
     pdl_trigger();
+    load_tab(tab, P.scr, 1);
+    __syncthreads();
+    // each warp fetches its next task index while the current task runs
+    uint32_t next = 0;
+    if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
     for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
-        t = __shfl_sync(MI_FULL_MASK, t, 0);
+        const uint32_t t = __shfl_sync(MI_FULL_MASK, next, 0);
         if (t >= ntasks) break;
-        const Task tk = decode(P.scr, 1, t);
+        if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
+        const Task tk = decode_tab<1>(tab, t);
         switch (min(tk.key - KEY_CLS, 5u)) {
             case 0: classic_task<1>(P, tk, wsm, nullptr); break;
             case 1: classic_task<2>(P, tk, wsm, nullptr); break;
@@ -517,14 +547,18 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
 // other's code and registers.
 __global__ void __launch_bounds__(256, 2) k_rg_comb(Params P) {
     const uint32_t lane = threadIdx.x & 31u;
+    __shared__ FamTab tab;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 5];
     pdl_trigger();
+    load_tab(tab, P.scr, 5);
+    __syncthreads();
+    uint32_t next = 0;  // the next task index, fetched while the current task runs
+    if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 5, 1u);
     for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 5, 1u);
-        t = __shfl_sync(MI_FULL_MASK, t, 0);
+        const uint32_t t = __shfl_sync(MI_FULL_MASK, next, 0);
         if (t >= ntasks) break;
-        const Task tk = decode(P.scr, 5, t);
+        if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 5, 1u);
+        const Task tk = decode_tab<5>(tab, t);
         const uint32_t ki = tk.key - KEY_CMB;
         if (ki == 0) comb_task<4>(P, tk);
         else if (ki == 1) comb_task<8>(P, tk);
@@ -541,15 +575,17 @@ __global__ void __launch_bounds__(256, 2) k_rg_c64(Params P) {
     extern __shared__ __align__(16) uint32_t smem32[];
     __shared__ uint32_t scr_warp[8];
     __shared__ uint32_t s_task[2];
+    __shared__ FamTab tab;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 3];
     pdl_trigger();
+    load_tab(tab, P.scr, 3);
     if (threadIdx.x == 0) s_task[0] = atomicAdd(P.scr + Scratch::QUEUE + 3, 1u);
     __syncthreads();
     for (uint32_t it = 0;; ++it) {
         const uint32_t t = s_task[it & 1];
         if (t >= ntasks) break;
         if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + 3, 1u);
-        classic_task<64>(P, decode(P.scr, 3, t), smem32, scr_warp);
+        classic_task<64>(P, decode_tab<3>(tab, t), smem32, scr_warp);
         __syncthreads();  // the next index is visible; shared memory is reused
     }
     pdl_wait();  // complete only after the task kernel launched before it
@@ -623,14 +659,18 @@ __device__ __forceinline__ void add_rows(const Params& P, const Task& tk) {
 
 __global__ void __launch_bounds__(256, 4) k_rg_add(Params P) {
     const uint32_t lane = threadIdx.x & 31u;
+    __shared__ FamTab tab;
     const uint32_t ntasks = P.scr[Scratch::NTASKS + 2];
     pdl_trigger();
+    load_tab(tab, P.scr, 2);
+    __syncthreads();
+    uint32_t next = 0;  // the next task index, fetched while the current task runs
+    if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
     for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
-        t = __shfl_sync(MI_FULL_MASK, t, 0);
+        const uint32_t t = __shfl_sync(MI_FULL_MASK, next, 0);
         if (t >= ntasks) break;
-        const Task tk = decode(P.scr, 2, t);
+        if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 2, 1u);
+        const Task tk = decode_tab<2>(tab, t);
         switch (tk.key - KEY_ADD) {
             case 0: add_short<1>(P, tk); break;
             case 1: add_short<2>(P, tk); break;
