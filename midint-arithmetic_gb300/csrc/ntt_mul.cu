@@ -8,8 +8,9 @@
 // Here every u64 limb is one digit; the product of two m-limb integers has
 // coefficients below m * 2^128 <= 2^139 (m <= 2048), so five primes
 // p_i < 2^30 (product 2^149.4) recover every coefficient exactly by CRT; when
-// 48-bit digits fit the same transform length (2 ceil(4m/3) <= L) the kernel
-// runs them on four primes instead (ntt_mul.cuh).  One CTA of L/8 threads
+// 40-bit digits fit the same transform length (2 ceil(8m/5) <= L, m <= 525)
+// the kernel runs them on three primes instead, else when 48-bit digits fit
+// (2 ceil(4m/3) <= L) on four (ntt_mul.cuh).  One CTA of L/8 threads
 // owns one instance (L = pow2ceil(2m) >= 256): for each prime it converts a
 // and b into the field, runs two forward transforms, multiplies pointwise and
 // runs the inverse transform (ntt32.cuh), leaving the residues in shared
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     extern __shared__ __align__(16) uint32_t smem32[];
     uint32_t* scratch = smem32 + ntt32::MulSmem<LG>::WORDS32;
     for (uint64_t inst = blockIdx.x; inst < n; inst += gridDim.x)
-        ntt32::mul_one<LG, NP == 4>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
+        ntt32::mul_one<LG, 5 - NP>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
 }
 
 template <int LG, int NP>
@@ -158,20 +159,23 @@ mi_status launch_mul_ntt(const uint64_t* a, const uint64_t* b, uint64_t* r, uint
     const uint32_t rlen = low ? m : 2 * m;
     uint32_t L = pow2ceil(2 * m);
     if (L < 256) L = 256;
-    // 48-bit digits on four primes when they fit the same length
-    const bool d48 = 2 * ntt32::ntt_digits(m, true) <= L;
+    // the digit mode with the fewest primes that fits the same length
+    const int np = 5 - ntt32::ntt_mode(m, m, L);
     const NttMulParams& P = base;
+#define NP_CASE(LGV)                                                                                  \
+    case (1u << LGV):                                                                                 \
+        return np == 3 ? launch_lg<LGV, 3>(a, b, r, n, m, rlen, P, st)                                \
+                       : (np == 4 ? launch_lg<LGV, 4>(a, b, r, n, m, rlen, P, st)                     \
+                                  : launch_lg<LGV, 5>(a, b, r, n, m, rlen, P, st));
     switch (L) {
-        case 256: return d48 ? launch_lg<8, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<8, 5>(a, b, r, n, m, rlen, P, st);
-        case 512: return d48 ? launch_lg<9, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<9, 5>(a, b, r, n, m, rlen, P, st);
-        case 1024:
-            return d48 ? launch_lg<10, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<10, 5>(a, b, r, n, m, rlen, P, st);
-        case 2048:
-            return d48 ? launch_lg<11, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<11, 5>(a, b, r, n, m, rlen, P, st);
-        case 4096:
-            return d48 ? launch_lg<12, 4>(a, b, r, n, m, rlen, P, st) : launch_lg<12, 5>(a, b, r, n, m, rlen, P, st);
+        NP_CASE(8)
+        NP_CASE(9)
+        NP_CASE(10)
+        NP_CASE(11)
+        NP_CASE(12)
         default: return set_error(MI_EINVAL, "ntt: %u limbs exceeds the maximum %u", m, kNttMaxLimbs);
     }
+#undef NP_CASE
 }
 
 mi_status launch_ntt_raw(const NttRawArgs& A, cudaStream_t st) {

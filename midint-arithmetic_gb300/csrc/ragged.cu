@@ -15,8 +15,10 @@
 //     previous kernel's last tasks leave idle (ragged_launch):
 //     * NTT products (shorter operand >= the crossover): a task is one CTA of
 //       256 threads = 2048/L products with L-point transforms (ntt_mul.cuh),
-//       one family with 64-bit digits on five primes and one with 48-bit
-//       digits on four for the products whose 48-bit digits fit the same L;
+//       one family with 64-bit digits on five primes, one with 48-bit
+//       digits on four for the products whose 48-bit digits fit the same L,
+//       and one with 40-bit digits on three for those whose 40-bit digits
+//       fit it (and whose shorter operand stays within the 3-prime bound);
 //     * classical products with a shorter operand of 9 to 128 limbs, a task
 //       per warp: 32/NT products whose shorter operand fits NT tiles of 8 u32
 //       limbs, broadcast to the group, while the longer one streams through
@@ -49,16 +51,18 @@ namespace rg {
 constexpr uint32_t kMaxLimbs = 1024;
 constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11, 64-bit digits (5 primes)
 constexpr int K_N48 = 4;         // the same with 48-bit digits (4 primes)
+constexpr int K_N40 = 4;         // the same with 40-bit digits (3 primes)
 constexpr int K_CLS = 13;        // NT = 1..16 (one chunk), NT = 32 x chunks = 1..8
 constexpr int K_ADD = 11;        // GS = 1..32 lanes of one limb; one warp over 2..32 rows of 32 limbs
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
 constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
 constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = KEY_CLS + K_CLS, KEY_C64 = KEY_ADD + K_ADD,
-              KEY_N48 = KEY_C64 + K_C64, KEY_CMB = KEY_N48 + K_N48;
-constexpr int K = KEY_CMB + K_CMB;
+              KEY_N48 = KEY_C64 + K_C64, KEY_CMB = KEY_N48 + K_N48, KEY_N40 = KEY_CMB + K_CMB;
+constexpr int K = KEY_N40 + K_N40;
 // families: NTT (64-bit digits), classical square products in a warp,
-// additions, classical in 64 threads, NTT with 48-bit digits, comb products
-constexpr int NFAM = 6;
+// additions, classical in 64 threads, NTT with 48-bit digits, comb products,
+// NTT with 40-bit digits
+constexpr int NFAM = 7;
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
@@ -106,10 +110,11 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min) 
         if (s >= ntt_min) {
             // L must hold all la+lb output limbs (the top limb is the carry out
             // of the last of the la+lb-1 coefficients), not only the
-            // coefficients; 48-bit digits on four primes when they fit the same L
+            // coefficients; 40-bit digits on three primes or 48-bit ones on
+            // four when they fit the same L
             const uint32_t lg = max(8u, ceil_log2(la + lb));
-            const uint32_t lg48 = max(8u, ceil_log2(ntt32::ntt_digits(la, true) + ntt32::ntt_digits(lb, true)));
-            return (lg48 == lg ? KEY_N48 : KEY_NTT) + (lg - 8);
+            const int dm = ntt32::ntt_mode(la, lb, 1u << lg);
+            return (dm == ntt32::DM40 ? KEY_N40 : (dm == ntt32::DM48 ? KEY_N48 : KEY_NTT)) + (lg - 8);
         }
         if (s > 128) return KEY_C64 + (2 * l + 511) / 512 - 1;  // 64-thread groups, chunks of 256 limbs
         if (s <= 8) {  // comb: 16 words of the longer operand per thread, 512 per pass of a warp
@@ -140,7 +145,8 @@ __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
     }
     if (key < KEY_N48) return 4u;                                     // classical: 256 threads / 64
     if (key < KEY_CMB) return 2048u >> (8 + key - KEY_N48);          // NTT, 48-bit digits
-    return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;           // comb: 32 / group
+    if (key < KEY_N40) return key - KEY_CMB < 3 ? 8u >> (key - KEY_CMB) : 1u;  // comb: 32 / group
+    return 2048u >> (8 + key - KEY_N40);                              // NTT, 40-bit digits
 }
 
 // Binning.  Blocks of classify and scatter own the same contiguous ranges of
@@ -168,13 +174,13 @@ __global__ void __launch_bounds__(256) k_classify(const mi_op* __restrict__ ops,
 
 // First key of family f (f = NFAM: the end of the key space).
 __host__ __device__ constexpr int fam_base(int f) {
-    return f == 0 ? KEY_NTT
-                  : (f == 1 ? KEY_CLS
-                            : (f == 2 ? KEY_ADD : (f == 3 ? KEY_C64 : (f == 4 ? KEY_N48 : (f == 5 ? KEY_CMB : K)))));
+    constexpr int base[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, KEY_N48, KEY_CMB, KEY_N40, K};
+    return base[f];
 }
 static_assert(fam_base(1) - fam_base(0) <= 32 && fam_base(2) - fam_base(1) <= 32 &&
                   fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32 &&
-                  fam_base(5) - fam_base(4) <= 32 && fam_base(6) - fam_base(5) <= 32,
+                  fam_base(5) - fam_base(4) <= 32 && fam_base(6) - fam_base(5) <= 32 &&
+                  fam_base(7) - fam_base(6) <= 32,
               "a family's keys fit one warp");
 
 // One warp per family scans its keys in c_order (shuffle scans): op offsets
@@ -289,7 +295,7 @@ __device__ __forceinline__ Task decode_tab(const FamTab& tab, uint32_t t) {
 
 // --- NTT family ----------------------------------------------------------------
 
-template <int LG, bool D48>
+template <int LG, int DM>
 __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32_t* sm, uint32_t* scr_warp) {
     constexpr int NT = (1 << LG) / 8;
     const uint32_t g = threadIdx.x / NT;
@@ -300,18 +306,20 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
     const bool busy = g < tk.count;
     mi_op op{};
     if (busy) op = P.ops[sorted[tk.first + g]];
-    ntt32::mul_one<LG, D48>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, busy ? P.out + op.r_off : nullptr,
+    ntt32::mul_one<LG, DM>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, busy ? P.out + op.r_off : nullptr,
                             op.la + op.lb, P.ntt, gsm, scr_warp);
 }
 
-// D48: the family of products with 48-bit digits on four primes (a kernel of
-// its own, so that neither digit mode's code raises the other's registers).
-// Two CTAs per SM at up to 128 registers: at three (85 registers) the 48-bit
-// products spilled 40-68 bytes at every transform length, and the list ran
-// 0.8 % slower (NTT band 0.896 against 0.878 ms on the 200000-op list).
-template <bool D48>
+// DM: the digit mode of the family (64-bit digits on five primes, 48-bit
+// on four, 40-bit on three: a kernel each, so that no digit mode's code
+// raises another's registers).  Two CTAs per SM at up to 128 registers: at
+// three (85 registers) the 48-bit products spilled 40-68 bytes at every
+// transform length, and the list ran 0.8 % slower (NTT band 0.896 against
+// 0.878 ms on the 200000-op list).
+template <int DM>
 __global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
-    constexpr int F = D48 ? 4 : 0;  // family
+    constexpr int F = DM == ntt32::DM64 ? 0 : (DM == ntt32::DM48 ? 4 : 6);  // family
+    constexpr int KEY0 = DM == ntt32::DM64 ? KEY_NTT : (DM == ntt32::DM48 ? KEY_N48 : KEY_N40);
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* scr_warp = smem + ntt32::MulSmem<11>::WORDS32;  // after the groups' shared memory
     __shared__ uint32_t s_task[2];  // this task and the next, fetched while this one runs
@@ -326,15 +334,15 @@ __global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
         if (t >= ntasks) break;
         if (threadIdx.x == 0) s_task[(it + 1) & 1] = atomicAdd(P.scr + Scratch::QUEUE + F, 1u);
         const Task tk = decode_tab<F>(tab, t);
-        switch (tk.key - (D48 ? KEY_N48 : KEY_NTT)) {
-            case 0: ntt_task<8, D48>(P, tk, smem, scr_warp); break;
-            case 1: ntt_task<9, D48>(P, tk, smem, scr_warp); break;
-            case 2: ntt_task<10, D48>(P, tk, smem, scr_warp); break;
-            default: ntt_task<11, D48>(P, tk, smem, scr_warp); break;
+        switch (tk.key - KEY0) {
+            case 0: ntt_task<8, DM>(P, tk, smem, scr_warp); break;
+            case 1: ntt_task<9, DM>(P, tk, smem, scr_warp); break;
+            case 2: ntt_task<10, DM>(P, tk, smem, scr_warp); break;
+            default: ntt_task<11, DM>(P, tk, smem, scr_warp); break;
         }
         __syncthreads();  // the next index is visible; this one is read by all
     }
-    if (D48) pdl_wait();  // complete only after the task kernel launched before it
+    if (DM != ntt32::DM64) pdl_wait();  // complete only after the task kernel launched before it
 }
 
 // --- classical family ----------------------------------------------------------
@@ -712,9 +720,11 @@ mi_status init_device() {
     for (int k = 0; k < K_ADD; ++k) order[KEY_ADD + k] = uint16_t(KEY_ADD + (K_ADD - 1 - k));
     for (int k = 0; k < K_C64; ++k) order[KEY_C64 + k] = uint16_t(KEY_C64 + (K_C64 - 1 - k));
     for (int k = 0; k < K_N48; ++k) order[KEY_N48 + k] = uint16_t(KEY_N48 + (K_N48 - 1 - k));
+    for (int k = 0; k < K_N40; ++k) order[KEY_N40 + k] = uint16_t(KEY_N40 + (K_N40 - 1 - k));
     MI_CUDA_TRY(cudaMemcpyToSymbol(c_order, order.data(), sizeof(uint16_t) * K));
-    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
-    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_classic, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kClsSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kC64Smem)));
     g_init[dev] = true;
@@ -758,10 +768,10 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     // disjoint results, so a kernel's blocks may start on the SMs that the
     // previous kernel's last tasks leave idle -- and waits for its predecessor
     // only before it completes, so that the last kernel completes after all.
-    k_rg_ntt<false><<<persistent_grid((const void*)k_rg_ntt<false>, kNttSmem), 256, kNttSmem, st>>>(P);
+    k_rg_ntt<0><<<persistent_grid((const void*)k_rg_ntt<0>, kNttSmem), 256, kNttSmem, st>>>(P);
     MI_CUDA_TRY(cudaGetLastError());
-    MI_CUDA_TRY(launch_pdl(k_rg_ntt<true>, persistent_grid((const void*)k_rg_ntt<true>, kNttSmem), 256, kNttSmem, st,
-                           P));
+    MI_CUDA_TRY(launch_pdl(k_rg_ntt<1>, persistent_grid((const void*)k_rg_ntt<1>, kNttSmem), 256, kNttSmem, st, P));
+    MI_CUDA_TRY(launch_pdl(k_rg_ntt<2>, persistent_grid((const void*)k_rg_ntt<2>, kNttSmem), 256, kNttSmem, st, P));
     MI_CUDA_TRY(launch_pdl(k_rg_classic, persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st, P));
     // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
     if (P.ntt_min > 129)

@@ -75,11 +75,26 @@ def test_mul_ntt_matches_oracle(ctx, devmem, m):
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [64, 96, 256, 384, 1024, 1536, 2048])
+# sizes whose 40-bit digits fit the transform length (three primes): 80 and
+# 320 limbs fill 256 and 1024 points exactly, 525 limbs is the largest
+# shorter operand the three primes keep exact (840 digits), 526 the first
+# that falls back to 48-bit digits on four
+D40_SIZES = [10, 40, 76, 80, 150, 160, 300, 320, 321, 400, 520, 525, 526]
+
+
+@pytest.mark.parametrize("m", D40_SIZES)
+def test_mul_ntt_40bit_digits_match_oracle(ctx, devmem, m):
+    a, b = carry_stress(6, m, seed=31 * m + 1)
+    assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
+
+
+@pytest.mark.parametrize("m", [64, 80, 96, 256, 320, 384, 525, 526, 1024, 1536, 2048])
 def test_mul_ntt_maximal_coefficients(ctx, devmem, m):
     # all-ones operands give the largest convolution coefficients (~m * 2^128
     # with 64-bit digits; 96, 384 and 1536 limbs fill their transform length
-    # exactly with 48-bit digits on four primes, coefficients ~(4m/3) * 2^96)
+    # exactly with 48-bit digits on four primes, coefficients ~(4m/3) * 2^96;
+    # 80 and 320 limbs fill it with 40-bit digits on three, and 525 limbs
+    # reach the three primes' bound, 840 (2^40 - 1)^2)
     a = np.full(3 * m, 0xFFFFFFFFFFFFFFFF, np.uint64)
     b = a.copy()
     b[m:2 * m] = 1

@@ -104,9 +104,12 @@ def test_ragged_matches_oracle(ctx, ntt_min):
 
 
 def test_ragged_all_ones_products(ctx):
-    kind = np.ones(40, np.uint32)
-    la = np.array([1024, 1000, 129, 128, 64, 7, 1024, 300, 256, 257] * 4, np.uint32)
-    lb = np.array([1024, 3, 128, 129, 1024, 1024, 1, 300, 1024, 200] * 4, np.uint32)
+    # 300 x 300, 525 x 525 and 525 x 700 run on 40-bit digits and three primes
+    # (525 limbs: the largest shorter operand they keep exact), 526 x 526 on
+    # 48-bit digits and four
+    kind = np.ones(56, np.uint32)
+    la = np.array([1024, 1000, 129, 128, 64, 7, 1024, 300, 256, 257, 525, 525, 526, 160] * 4, np.uint32)
+    lb = np.array([1024, 3, 128, 129, 1024, 1024, 1, 300, 1024, 200, 525, 700, 526, 160] * 4, np.uint32)
     ops, pool, out_limbs = W.pack_ops(kind, la, lb, 9)
     pool[:] = np.uint64(2**64 - 1)
     old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN)
