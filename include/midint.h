@@ -91,7 +91,13 @@ mi_status mi_ctx_set_crossover(mi_ctx ctx, uint32_t ragged_ntt_min, uint32_t pla
  * that the project's autotuner measured and committed; these calls override
  * one entry (the autotuner itself sweeps candidates through them).
  *   MI_TUNE_PLAIN_NTT_MIN    cls ignored; value 1..2049 (as plain_ntt_min)
- *   MI_TUNE_RAGGED_NTT_MIN   cls ignored; value 1..257 (as ragged_ntt_min)
+ *   MI_TUNE_RAGGED_NTT_MIN   cls 0: value 1..257 (as ragged_ntt_min);
+ *                            cls 1: value 1..257, products whose NTT runs
+ *                            on 40-bit digits and three primes (their
+ *                            digits fill at most 5/8 of the transform
+ *                            length) use the NTT kernel from this many
+ *                            limbs of the shorter operand on, even below
+ *                            ragged_ntt_min
  *   MI_TUNE_LO_NTT_MIN       cls ignored; value 1..2049: mi_mul_lo_u64 and
  *                            the u64 gpuMultiply wrapper compute the low
  *                            half with the NTT kernel from this many limbs

@@ -16,9 +16,11 @@ Knobs:
   * the same for the low half (mi_mul_lo_u64), 256 to 2048 limbs;
   * the same for the fused composite (mi_poly_u64: four classical low halves
     against four low halves on transforms), 64 to 2048 limbs;
-  * ragged classical/NTT crossover: the 200000-op mixed ragged workload (40%
+  * ragged classical/NTT crossovers: the 200000-op mixed ragged workload (40%
     adds, operand bits log-uniform in [256, 65536]) timed end to end for every
-    candidate threshold; the fastest wins;
+    candidate pair of thresholds (the shorter operand from which every
+    product uses the NTT, and the one from which products whose NTT runs on
+    40-bit digits and three primes do); the fastest pair wins;
   * host-buffer calls: chunk count of the copy/compute pipeline, or zero-copy
     kernels on mapped pinned buffers, timed on the multiplication batch.
 
@@ -192,7 +194,7 @@ def tune_poly_crossover(ctx, stream, dev) -> tuple[int, dict]:
     return pick, record
 
 
-def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
+def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[tuple[int, int], dict]:
     import torch
 
     import midint
@@ -208,16 +210,22 @@ def tune_ragged_crossover(ctx, stream, dev, n_ops: int) -> tuple[int, dict]:
     sp = stream.cuda_stream
     record = {}
     ref = None
-    for th in (32, 64, 96, 128, 160, 192, 224, 256, 257):
-        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, th)
-        ms = _timer(lambda: ctx.ragged_run(d_ops, n_ops, d_in, d_out, scr, sb, carry=d_c, stream=sp), 5, 2, stream)
-        out = d_out.cpu().numpy()
-        if ref is None:
-            ref = out.copy()
-        elif not np.array_equal(out, ref):
-            raise SystemExit(f"autotune: ragged results differ at threshold {th}")
-        record[str(th)] = {"ms": ms}
-    pick = int(min(record, key=lambda k: record[k]["ms"]))
+    for th in (64, 96, 112, 128, 144, 160, 192, 257):
+        for th40 in (32, 48, 64, 80, 96, 112, 128):
+            if th40 >= th and th40 != 32:
+                continue  # the same as th40 = th
+            ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, th)
+            ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 1, min(th40, th))
+            ms = _timer(lambda: ctx.ragged_run(d_ops, n_ops, d_in, d_out, scr, sb, carry=d_c, stream=sp), 5, 2,
+                        stream)
+            out = d_out.cpu().numpy()
+            if ref is None:
+                ref = out.copy()
+            elif not np.array_equal(out, ref):
+                raise SystemExit(f"autotune: ragged results differ at thresholds {th}, {th40}")
+            record[f"{th}/{min(th40, th)}"] = {"ms": ms}
+    best = min(record, key=lambda k: record[k]["ms"])
+    pick = tuple(int(v) for v in best.split("/"))
     del d_ops, d_in, d_out, d_c, scr
     torch.cuda.empty_cache()
     return pick, {"ops": n_ops, "candidates": record}
@@ -302,8 +310,10 @@ constexpr uint32_t kLoNttMin = {lo};
 // products on the NTT (2049 = never).
 constexpr uint32_t kPolyNttMin = {poly};
 // Ragged runs: products whose shorter operand has at least this many u64
-// limbs use the NTT kernel (1..257).
+// limbs use the NTT kernel (1..257), and so do those from kRaggedNtt40Min
+// limbs whose NTT runs on 40-bit digits and three primes.
 constexpr uint32_t kRaggedNttMin = {ragged};
+constexpr uint32_t kRaggedNtt40Min = {ragged40};
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {{{add}}};
@@ -329,7 +339,8 @@ def render_header(device: str, date: str, picks: dict) -> str:
 
     return HEADER.format(device=device, date=date, plain=picks["plain_ntt_min"], lo=picks["lo_ntt_min"],
                          poly=picks["poly_ntt_min"],
-                         ragged=picks["ragged_ntt_min"], chunks=join(picks["host_chunks"]),
+                         ragged=picks["ragged_ntt_min"], ragged40=picks["ragged_ntt40_min"],
+                         chunks=join(picks["host_chunks"]),
                          zero_copy=join(picks["host_zero_copy"]), zc_blocks=join(picks["host_zc_blocks"]),
                          add=join(picks["add_thread_bytes"]))
 
@@ -360,6 +371,7 @@ def main():
     picks.setdefault("host_zc_blocks", [0, 0])
     picks.setdefault("lo_ntt_min", 2049)
     picks.setdefault("poly_ntt_min", 2049)
+    picks.setdefault("ragged_ntt40_min", picks["ragged_ntt_min"])
     record = {k: old.get(k) for k in ("add", "plain_crossover", "lo_crossover", "poly_crossover", "ragged_crossover",
                                       "host")}
     if "add" in only:
@@ -371,7 +383,8 @@ def main():
     if "poly" in only:
         picks["poly_ntt_min"], record["poly_crossover"] = tune_poly_crossover(ctx, stream, dev)
     if "ragged" in only:
-        picks["ragged_ntt_min"], record["ragged_crossover"] = tune_ragged_crossover(ctx, stream, dev, args.ragged_ops)
+        (picks["ragged_ntt_min"], picks["ragged_ntt40_min"]), record["ragged_crossover"] = tune_ragged_crossover(
+            ctx, stream, dev, args.ragged_ops)
     if "host" in only:
         picks["host_chunks"], picks["host_zero_copy"], picks["host_zc_blocks"], record["host"] = tune_host(ctx)
     ctx.close()

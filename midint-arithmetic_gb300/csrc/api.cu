@@ -432,8 +432,9 @@ mi_status mi_ctx_set_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t value) 
             ctx->plain_ntt_min = value;
             return MI_OK;
         case MI_TUNE_RAGGED_NTT_MIN:
+            if (cls > 1) return set_error(MI_EINVAL, "ragged crossover class %u not 0 or 1", cls);
             if (value < 1 || value > 257) return set_error(MI_EINVAL, "ragged_ntt_min %u outside 1..257", value);
-            ctx->ragged_ntt_min = value;
+            (cls == 0 ? ctx->ragged_ntt_min : ctx->ragged_ntt40_min) = value;
             return MI_OK;
         case MI_TUNE_LO_NTT_MIN:
             if (value < 1 || value > kNttMaxLimbs + 1)
@@ -487,7 +488,10 @@ mi_status mi_ctx_get_tuning(mi_ctx ctx, int knob, uint32_t cls, uint32_t* value)
     if (ctx == nullptr || value == nullptr) return set_error(MI_EINVAL, "null context or value");
     switch (knob) {
         case MI_TUNE_PLAIN_NTT_MIN: *value = ctx->plain_ntt_min; return MI_OK;
-        case MI_TUNE_RAGGED_NTT_MIN: *value = ctx->ragged_ntt_min; return MI_OK;
+        case MI_TUNE_RAGGED_NTT_MIN:
+            if (cls > 1) return set_error(MI_EINVAL, "ragged crossover class %u not 0 or 1", cls);
+            *value = cls == 0 ? ctx->ragged_ntt_min : ctx->ragged_ntt40_min;
+            return MI_OK;
         case MI_TUNE_LO_NTT_MIN: *value = ctx->lo_ntt_min; return MI_OK;
         case MI_TUNE_POLY_NTT_MIN: *value = ctx->poly_ntt_min; return MI_OK;
         case MI_TUNE_ADD_THREAD_BYTES:

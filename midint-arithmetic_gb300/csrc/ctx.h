@@ -31,6 +31,7 @@ struct mi_ctx_s {
     // u64 limbs go through the NTT kernel (at most 257: classical groups hold
     // 256 limbs of the shorter operand)
     uint32_t ragged_ntt_min = mi::tuned::kRaggedNttMin;
+    uint32_t ragged_ntt40_min = mi::tuned::kRaggedNtt40Min;
     // mi_mul_u64: square products of at least this many u64 limbs use the NTT
     uint32_t plain_ntt_min = mi::tuned::kPlainNttMin;
     // mi_mul_lo_u64 and the u64 gpuMultiply wrapper: low halves of products

@@ -82,9 +82,12 @@ def edge_ops(seed, n_rand=600):
     return W.pack_ops(np.array(kind, np.uint32), np.array(la, np.uint32), np.array(lb, np.uint32), seed)
 
 
-@pytest.mark.parametrize("ntt_min", [257, 200, 129, 64, 1])
-def test_ragged_matches_oracle(ctx, ntt_min):
-    ops, pool, out_limbs = edge_ops(seed=ntt_min)
+# (ntt_min, ntt40_min): the shorter operand from which every product takes
+# the NTT, and from which products whose NTT runs on 40-bit digits do
+@pytest.mark.parametrize("ntt_min,ntt40_min", [(257, 257), (257, 1), (200, 64), (129, 129), (128, 80), (64, 64),
+                                               (1, 1)])
+def test_ragged_matches_oracle(ctx, ntt_min, ntt40_min):
+    ops, pool, out_limbs = edge_ops(seed=ntt_min + ntt40_min)
     # worst-case carries for some adds: a all ones, b = 1
     for i in range(0, ops.size, 7):
         if ops["kind"][i] == 0:
@@ -93,12 +96,14 @@ def test_ragged_matches_oracle(ctx, ntt_min):
             pool[ao:ao + la] = np.uint64(2**64 - 1)
             pool[bo:bo + lb] = 0
             pool[bo] = 1
-    old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN)
+    old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN), ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN, 1)
     ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, ntt_min)
+    ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 1, ntt40_min)
     try:
         out, carry, invalid = run_ragged(ctx, ops, pool, out_limbs)
     finally:
-        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, old)
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, old[0])
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 1, old[1])
     assert invalid == 0
     oracle_check(ops, pool, out, carry)
 
@@ -113,11 +118,14 @@ def test_ragged_all_ones_products(ctx):
     ops, pool, out_limbs = W.pack_ops(kind, la, lb, 9)
     pool[:] = np.uint64(2**64 - 1)
     old = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN)
-    for ntt_min in (257, 200, 129, 1):
+    old40 = ctx.get_tuning(midint.TUNE_RAGGED_NTT_MIN, 1)
+    for ntt_min, ntt40_min in ((257, 257), (200, 200), (129, 129), (257, 1), (1, 1)):
         ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, ntt_min)
+        ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 1, ntt40_min)
         out, carry, _ = run_ragged(ctx, ops, pool, out_limbs)
         oracle_check(ops, pool, out, carry)
     ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 0, old)
+    ctx.set_tuning(midint.TUNE_RAGGED_NTT_MIN, 1, old40)
 
 
 def test_ragged_invalid_ops_are_skipped(ctx):

@@ -26,6 +26,7 @@ def test_table_matches_record():
     assert table["kLoNttMin"] == picks["lo_ntt_min"]
     assert table["kPolyNttMin"] == picks["poly_ntt_min"]
     assert table["kRaggedNttMin"] == picks["ragged_ntt_min"]
+    assert table["kRaggedNtt40Min"] == picks["ragged_ntt40_min"]
     assert table["kAddThreadBytes"] == picks["add_thread_bytes"]
     assert table["kHostChunks"] == picks["host_chunks"]
     assert table["kHostZeroCopy"] == picks["host_zero_copy"]
@@ -38,6 +39,7 @@ def test_picks_are_accepted_values():
     assert 1 <= picks["lo_ntt_min"] <= 2049
     assert 1 <= picks["poly_ntt_min"] <= 2049
     assert 1 <= picks["ragged_ntt_min"] <= 257
+    assert 1 <= picks["ragged_ntt40_min"] <= picks["ragged_ntt_min"]
     assert len(picks["add_thread_bytes"]) == 13 and set(picks["add_thread_bytes"]) <= {16, 32, 64}
     assert all(1 <= c <= 64 for c in picks["host_chunks"])
     assert all(0 <= z <= 3 for z in picks["host_zero_copy"])
