@@ -66,7 +66,8 @@ constexpr int NFAM = 7;
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int kAddRowBatch = 4;    // rows of 32 limbs per batch of loads (two batches in flight)
-constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
+// A, B planes, per-thread slots, and a second B plane buffer (32-thread products over rounds)
+constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T + 256;
 constexpr int C64_GROUP_WORDS = 512 + 512 + 64 * classic::PER_T;  // the same for one 64-thread group
 
 // Keys of each family in descending cost order (filled once per device).
@@ -432,6 +433,205 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     if (valid) classic::store_pairs(rr, chunks * W + t * T, rlen, pend);
 }
 
+// --- 32-thread products over rounds of output blocks --------------------------
+//
+// A product whose shorter operand y has nby <= 32 blocks (of T words) and
+// whose longer operand x has `chunks` chunks of 32 blocks, one warp.  Round c
+// gives lane t the whole anti-diagonal of output block 32c + t:
+//   D = sum over k < nby of y_k * x_(32c + t - k),
+// whose x blocks lie in chunk c (k <= t) or chunk c - 1 (k > t).  Both chunks
+// sit in shared memory (two plane buffers, alternating), so a lane's tiles of
+// one round all land on one output block: one accumulator, no snapshot, and
+// one output block per lane per round.  Only the first round wraps: chunk 0's
+// lower anti-diagonals (blocks 0..31) share the lanes with the last chunk's
+// upper ones (blocks 32 chunks + t), split by a snapshot as in the square
+// product; the upper values wait in shared memory for the last round.  Each
+// round resolves its blocks L_t + H_(t-1) + O_(t-2) with the words of the
+// previous round's last two anti-diagonals and its carries, so the blocks
+// come out final in order.  (A chunked square product per chunk spends a
+// snapshot per step and a two-block resolution per lane on every chunk.)
+
+// Warp area (CLS_WARP_WORDS words): y blocks [0, 256), plane buffer 0
+// [256, 512), the snapshot slots [512, 1792), plane buffer 1 [1792, 2048).
+
+// Writes thread t's two 16-byte slots of a chunk (load_chunk_regs<32>) into a
+// plane buffer: half h of block j at slot h*32 + j.
+__device__ __forceinline__ void store_planes32(uint4* buf, const uint4 (&q)[classic::T / 4], uint32_t t) {
+#pragma unroll
+    for (int it = 0; it < classic::T / 4; ++it) {
+        const uint32_t v = t + uint32_t(it) * 32;
+        buf[(v & 1) * 32 + (v >> 1)] = q[it];
+    }
+}
+
+// One round's tiles: lane t accumulates y_k * x-block (t - k) mod 32 of `cur`
+// (k <= t) or `prev` (k > t), k < nby.  SNAP: the wrap round, whose lane t
+// snapshots its accumulator at step min(t, nby - 1) (its lower anti-diagonal
+// complete).
+template <bool SNAP>
+__device__ __forceinline__ void rect_tiles(const uint32_t* gA, const uint4* cur, const uint4* prev, uint2* slots,
+                                           uint32_t t, uint32_t nby, classic::DiagAcc& s) {
+    using classic::T;
+#pragma unroll
+    for (int w = 0; w < 2 * T; ++w) s.a[w] = 0;
+#pragma unroll
+    for (int w = 0; w < 2 * T - 2; ++w) s.b[w] = 0;
+#pragma unroll
+    for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
+    const uint32_t snap_k = t < nby ? t : nby - 1;
+#pragma unroll 4
+    for (uint32_t k = 0; k < nby; ++k) {
+        const uint32_t j = (t - k) & 31u;
+        const uint4* src = k <= t ? cur : prev;
+        const uint4 a0 = reinterpret_cast<const uint4*>(gA + k * T)[0];
+        const uint4 a1 = reinterpret_cast<const uint4*>(gA + k * T)[1];
+        const uint4 b0 = src[j], b1 = src[32 + j];
+        uint32_t A[T], B[T];
+        A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
+        A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
+        B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
+        B[4] = b1.x; B[5] = b1.y; B[6] = b1.z; B[7] = b1.w;
+        classic::tile_mac(A, B, s);
+        if (SNAP && k == snap_k) {
+#pragma unroll
+            for (int w = 0; w < T; ++w) slots[w * 32 + t] = make_uint2(s.a[2 * w], s.a[2 * w + 1]);
+#pragma unroll
+            for (int w = 0; w < T - 1; ++w) slots[(T + w) * 32 + t] = make_uint2(s.b[2 * w], s.b[2 * w + 1]);
+#pragma unroll
+            for (int w = 0; w < T / 2; ++w)
+                slots[(2 * T - 1 + w) * 32 + t] = make_uint2(s.cc[2 * w], s.cc[2 * w + 1]);
+            slots[(2 * T - 1 + T / 2) * 32 + t] = make_uint2(s.cc[T], 0u);
+        }
+    }
+}
+
+// Output block blk0 + t from lane t's anti-diagonal value D (L = words 0..7,
+// H = 8..15, O = 16): L_t + H_(t-1) + O_(t-2), lanes 0 and 1 taking the words
+// of the previous round's lanes 31 and 30 from `cs` (zeros in the first
+// round), then carried: kprev is the previous round's last add3 carry (0..2),
+// cprev its lookahead carry out; both are updated for the next round.  Stores
+// the block (clipped to rlen words) and leaves lane 31's H and O and lane
+// 30's O in `cs`.
+__device__ __forceinline__ void rect_epilogue(const uint32_t (&D)[classic::ACC], uint32_t* cs, uint32_t t,
+                                              bool first, uint32_t& kprev, uint32_t& cprev, uint32_t* rr,
+                                              uint32_t blk0, uint32_t rlen) {
+    using classic::T;
+    const uint32_t src1 = (t - 1) & 31u, src2 = (t - 2) & 31u;
+    uint32_t L[T], H[T], r[T];
+#pragma unroll
+    for (int w = 0; w < T; ++w) {
+        const uint32_t v = __shfl_sync(MI_FULL_MASK, D[T + w], src1);
+        H[w] = t ? v : (first ? 0u : cs[w]);
+        L[w] = D[w];
+    }
+    const uint32_t o = __shfl_sync(MI_FULL_MASK, D[2 * T], src2);
+    const uint32_t O = t >= 2 ? o : (first ? 0u : cs[t == 0 ? T + 1 : T]);
+    __syncwarp();  // lanes 0 and 1 have read the previous round's words
+    if (t == 31) {
+#pragma unroll
+        for (int w = 0; w < T; ++w) cs[w] = D[T + w];
+        cs[T] = D[2 * T];
+    }
+    if (t == 30) cs[T + 1] = D[2 * T];
+    const uint32_t k = classic::add3_block(L, H, O, r);
+    const uint32_t up = __shfl_up_sync(MI_FULL_MASK, k, 1);
+    const uint32_t e = classic::add_word_block(r, t ? up : kprev);
+    uint32_t cout;
+    const uint32_t c = group_carry<32>(e != 0, classic::all_ones(r), cprev, &cout, nullptr);
+    classic::add_word_block(r, c);
+    classic::store_pairs(rr, (blk0 + t) * T, rlen, r);
+    kprev = __shfl_sync(MI_FULL_MASK, k, 31);
+    cprev = cout;
+}
+
+__device__ __forceinline__ void rect32_task(const Params& P, const Task& tk, uint32_t* sm) {
+    using classic::ACC;
+    using classic::PAIRS;
+    using classic::T;
+    const uint32_t t = threadIdx.x & 31u;
+    const uint32_t chunks = tk.key - KEY_CLS - 4;  // keys KEY_CLS + 5.. : 1..8 chunks of 32 blocks
+    const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
+    const mi_op op = P.ops[sorted[tk.first]];
+    const bool a_long = op.la >= op.lb;
+    const uint32_t* x = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.a_off : op.b_off));
+    const uint32_t* y = reinterpret_cast<const uint32_t*>(P.in + (a_long ? op.b_off : op.a_off));
+    const uint32_t nx = 2 * (a_long ? op.la : op.lb), ny = 2 * (a_long ? op.lb : op.la);
+    uint32_t* rr = reinterpret_cast<uint32_t*>(P.out + op.r_off);
+    const uint32_t rlen = 2 * (op.la + op.lb);
+    const uint32_t nby = (ny + T - 1) / T;
+    constexpr uint32_t W = 32 * T;  // words of a chunk
+    uint32_t* gA = sm;
+    uint4* buf0 = reinterpret_cast<uint4*>(sm + 256);
+    uint2* slots = reinterpret_cast<uint2*>(sm + 512);
+    uint4* buf1 = reinterpret_cast<uint4*>(sm + 512 + 32 * classic::PER_T);
+    uint32_t* cs = sm + 512 + 2 * 10 * 32;  // snapshot pairs 10.. of lanes 0..4, free after the wrap round
+    const uint32_t last = chunks - 1;
+
+    uint4 q[T / 4];
+    load_chunk_regs<32>(q, y, ny, 0, t);
+#pragma unroll
+    for (int it = 0; it < T / 4; ++it) reinterpret_cast<uint4*>(gA)[t + it * 32] = q[it];
+    load_chunk_regs<32>(q, x, nx, 0, t);
+    store_planes32(buf0, q, t);
+    if (last) {
+        load_chunk_regs<32>(q, x, nx, last * W, t);
+        store_planes32(buf1, q, t);
+    }
+    uint4 nxt[T / 4];
+    if (chunks > 2) load_chunk_regs<32>(nxt, x, nx, W, t);  // chunk 1; buf1 holds the last chunk until then
+    __syncwarp();
+
+    // the wrap round: chunk 0's lower anti-diagonals and the last chunk's upper ones
+    classic::DiagAcc s;
+    rect_tiles<true>(gA, buf0, last ? buf1 : buf0, slots, t, nby, s);
+    uint32_t d1[ACC], d2[ACC];
+    {
+        uint32_t snap[2 * PAIRS];
+#pragma unroll
+        for (int w = 0; w < PAIRS; ++w) {
+            const uint2 v = slots[w * 32 + t];
+            snap[2 * w] = v.x;
+            snap[2 * w + 1] = v.y;
+        }
+        classic::fold(snap, snap + 2 * T, snap + 4 * T - 2, d1);
+        classic::fold(s.a, s.b, s.cc, d2);
+        sub_cc(d2[0], d1[0]);
+#pragma unroll
+        for (int w = 1; w < ACC - 1; ++w) subc_cc(d2[w], d1[w]);
+        subc(d2[ACC - 1], d1[ACC - 1]);
+    }
+#pragma unroll
+    for (int w = 0; w < ACC / 2; ++w) slots[w * 32 + t] = make_uint2(d2[2 * w], d2[2 * w + 1]);  // own pairs 0..8
+    slots[(ACC / 2) * 32 + t] = make_uint2(d2[ACC - 1], 0u);
+    uint32_t kprev = 0, cprev = 0;
+    rect_epilogue(d1, cs, t, true, kprev, cprev, rr, 0, rlen);
+
+    for (uint32_t c = 1; c < chunks; ++c) {
+        uint4* cur = (c & 1) ? buf1 : buf0;
+        const uint4* prev = (c & 1) ? buf0 : buf1;
+        if (c > 1 || chunks > 2) {  // chunk c replaces chunk c - 2 (or, for c = 1, the last chunk)
+            __syncwarp();
+            store_planes32(cur, nxt, t);
+            if (c + 1 < chunks) load_chunk_regs<32>(nxt, x, nx, (c + 1) * W, t);
+        }
+        __syncwarp();
+        rect_tiles<false>(gA, cur, prev, slots, t, nby, s);
+        classic::fold(s.a, s.b, s.cc, d1);
+        rect_epilogue(d1, cs, t, false, kprev, cprev, rr, c * 32, rlen);
+    }
+    // the last chunk's upper anti-diagonals, kept since the wrap round
+#pragma unroll
+    for (int w = 0; w < ACC / 2; ++w) {
+        const uint2 v = slots[w * 32 + t];
+        d2[2 * w] = v.x;
+        d2[2 * w + 1] = v.y;
+    }
+    d2[ACC - 1] = slots[(ACC / 2) * 32 + t].x;
+    __syncwarp();  // the last round's words in cs are visible
+    rect_epilogue(d2, cs, t, false, kprev, cprev, rr, chunks * 32, rlen);
+    __syncwarp();  // the warp's area is reused by its next task
+}
+
 // Comb products, shorter operand y of at most 8 limbs (16 words, held in
 // registers by every thread of the group): thread t multiplies its 16 words
 // of the longer operand x by y (row carry chains in 64-bit arithmetic), keeps
@@ -546,7 +746,7 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
             case 2: classic_task<4>(P, tk, wsm, nullptr); break;
             case 3: classic_task<8>(P, tk, wsm, nullptr); break;
             case 4: classic_task<16>(P, tk, wsm, nullptr); break;
-            default: classic_task<32>(P, tk, wsm, nullptr); break;
+            default: rect32_task(P, tk, wsm); break;
         }
         __syncwarp();
     }
