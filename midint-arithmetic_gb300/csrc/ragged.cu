@@ -52,22 +52,24 @@ constexpr uint32_t kMaxLimbs = 1024;
 constexpr int K_NTT = 4;         // transform length 2^8 .. 2^11, 64-bit digits (5 primes)
 constexpr int K_N48 = 4;         // the same with 48-bit digits (4 primes)
 constexpr int K_N40 = 4;         // the same with 40-bit digits (3 primes)
-constexpr int K_CLS = 13;        // NT = 1..16 (one chunk), NT = 32 x chunks = 1..8
+constexpr int K_CLS = 5;         // NT = 1..16 (one chunk)
 constexpr int K_ADD = 11;        // GS = 1..32 lanes of one limb; one warp over 2..32 rows of 32 limbs
 constexpr int K_C64 = 4;         // classical, 64-thread groups: chunks = 1..4
 constexpr int K_CMB = 7;         // comb, shorter operand <= 8 limbs: groups of 4, 8, 16, 32 x passes 1..4
+constexpr int K_R32 = 8;         // classical, 32 threads in rounds: chunks of 32 blocks = 1..8
 constexpr int KEY_NTT = 0, KEY_CLS = K_NTT, KEY_ADD = KEY_CLS + K_CLS, KEY_C64 = KEY_ADD + K_ADD,
-              KEY_N48 = KEY_C64 + K_C64, KEY_CMB = KEY_N48 + K_N48, KEY_N40 = KEY_CMB + K_CMB;
-constexpr int K = KEY_N40 + K_N40;
-// families: NTT (64-bit digits), classical square products in a warp,
-// additions, classical in 64 threads, NTT with 48-bit digits, comb products,
-// NTT with 40-bit digits
-constexpr int NFAM = 7;
+              KEY_N48 = KEY_C64 + K_C64, KEY_CMB = KEY_N48 + K_N48, KEY_N40 = KEY_CMB + K_CMB,
+              KEY_R32 = KEY_N40 + K_N40;
+constexpr int K = KEY_R32 + K_R32;
+// families: NTT (64-bit digits), classical square products of groups of up
+// to 16 threads, additions, classical in 64 threads, NTT with 48-bit digits,
+// comb products, NTT with 40-bit digits, classical in 32 threads over rounds
+constexpr int NFAM = 8;
 constexpr uint32_t KEY_INVALID = 0xffffffffu;
 constexpr uint32_t kAddRowOps = 4;  // additions of more than 32 limbs per warp task
 constexpr int kAddRowBatch = 4;    // rows of 32 limbs per batch of loads (two batches in flight)
-// A, B planes, per-thread slots, and a second B plane buffer (32-thread products over rounds)
-constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T + 256;
+constexpr int CLS_WARP_WORDS = 256 + 256 + 32 * classic::PER_T;  // A, B planes, per-thread slots
+constexpr int R32_WARP_WORDS = CLS_WARP_WORDS + 256;  // the same and a second B plane buffer
 constexpr int C64_GROUP_WORDS = 512 + 512 + 64 * classic::PER_T;  // the same for one 64-thread group
 
 // Keys of each family in descending cost order (filled once per device).
@@ -132,17 +134,15 @@ __device__ __forceinline__ uint32_t classify(const mi_op& op, uint32_t ntt_min, 
         const uint32_t nbs = (2 * s + 7) / 8, nbl = (2 * l + 7) / 8;
         const uint32_t ntl = ceil_log2(max(nbs, min(nbl, 32u)));  // NT = 2^ntl <= 32
         if (ntl < 5) return KEY_CLS + ntl;  // NT >= nbl: one chunk
-        return KEY_CLS + 5 + (nbl + 31) / 32 - 1;  // NT = 32, nbl <= 256: 1..8 chunks
+        return KEY_R32 + (nbl + 31) / 32 - 1;  // NT = 32, nbl <= 256: 1..8 chunks
     }
     return KEY_INVALID;
 }
 
 __host__ __device__ __forceinline__ uint32_t ops_per_task(uint32_t key) {
+    if (key >= KEY_R32) return 1u;                                    // classical, 32 threads over rounds
     if (key < KEY_CLS) return 2048u >> (8 + key - KEY_NTT);          // NTT: 256 threads / (L/8)
-    if (key < KEY_ADD) {                                              // classical: one warp
-        const uint32_t k = key - KEY_CLS;
-        return k < 5 ? 32u >> k : 1u;
-    }
+    if (key < KEY_ADD) return 32u >> (key - KEY_CLS);                // classical: one warp of 32/NT groups
     if (key < KEY_C64) {                                              // add: one warp
         const uint32_t k = key - KEY_ADD;
         return k < 6 ? 32u >> k : kAddRowOps;
@@ -178,13 +178,13 @@ __global__ void __launch_bounds__(256) k_classify(const mi_op* __restrict__ ops,
 
 // First key of family f (f = NFAM: the end of the key space).
 __host__ __device__ constexpr int fam_base(int f) {
-    constexpr int base[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, KEY_N48, KEY_CMB, KEY_N40, K};
+    constexpr int base[NFAM + 1] = {KEY_NTT, KEY_CLS, KEY_ADD, KEY_C64, KEY_N48, KEY_CMB, KEY_N40, KEY_R32, K};
     return base[f];
 }
 static_assert(fam_base(1) - fam_base(0) <= 32 && fam_base(2) - fam_base(1) <= 32 &&
                   fam_base(3) - fam_base(2) <= 32 && fam_base(4) - fam_base(3) <= 32 &&
                   fam_base(5) - fam_base(4) <= 32 && fam_base(6) - fam_base(5) <= 32 &&
-                  fam_base(7) - fam_base(6) <= 32,
+                  fam_base(7) - fam_base(6) <= 32 && fam_base(8) - fam_base(7) <= 32,
               "a family's keys fit one warp");
 
 // One warp per family scans its keys in c_order (shuffle scans): op offsets
@@ -380,7 +380,7 @@ __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, ui
     const uint32_t g = lane / NT, t = lane % NT;
     const bool valid = g < tk.count;
     if (!WIDE && !valid) return;  // warp groups synchronise only among their own lanes
-    const uint32_t chunks = WIDE ? tk.key - KEY_C64 + 1 : (tk.key - KEY_CLS < 5 ? 1u : tk.key - KEY_CLS - 4);
+    const uint32_t chunks = WIDE ? tk.key - KEY_C64 + 1 : 1u;
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     mi_op op{};
     if (valid) op = P.ops[sorted[tk.first + g]];
@@ -549,7 +549,7 @@ __device__ __forceinline__ void rect32_task(const Params& P, const Task& tk, uin
     using classic::PAIRS;
     using classic::T;
     const uint32_t t = threadIdx.x & 31u;
-    const uint32_t chunks = tk.key - KEY_CLS - 4;  // keys KEY_CLS + 5.. : 1..8 chunks of 32 blocks
+    const uint32_t chunks = tk.key - KEY_R32 + 1;  // 1..8 chunks of 32 blocks
     const uint32_t* sorted = P.scr + Scratch::sorted(P.n_ops);
     const mi_op op = P.ops[sorted[tk.first]];
     const bool a_long = op.la >= op.lb;
@@ -740,15 +740,40 @@ __global__ void __launch_bounds__(256, 2) k_rg_classic(Params P) {
         if (t >= ntasks) break;
         if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 1, 1u);
         const Task tk = decode_tab<1>(tab, t);
-        switch (min(tk.key - KEY_CLS, 5u)) {
+        switch (tk.key - KEY_CLS) {
             case 0: classic_task<1>(P, tk, wsm, nullptr); break;
             case 1: classic_task<2>(P, tk, wsm, nullptr); break;
             case 2: classic_task<4>(P, tk, wsm, nullptr); break;
             case 3: classic_task<8>(P, tk, wsm, nullptr); break;
-            case 4: classic_task<16>(P, tk, wsm, nullptr); break;
-            default: rect32_task(P, tk, wsm); break;
+            default: classic_task<16>(P, tk, wsm, nullptr); break;
         }
         __syncwarp();
+    }
+    pdl_wait();  // complete only after the task kernel launched before it
+}
+
+// 32-thread products over rounds (shorter operand of 17..128 limbs below the
+// NTT crossover, or a longer one of more than 64): a family and a kernel of
+// their own.  Two CTAs per SM at up to 128 registers: at three (80 registers)
+// the tile loop could no longer read a few steps' operands ahead, and the
+// list ran 1.62 ms (unrolled 2 deep, 48 bytes spilled) or 1.70 ms (not
+// unrolled) against 1.51 ms.
+__global__ void __launch_bounds__(256, 2) k_rg_r32(Params P) {
+    extern __shared__ __align__(16) uint32_t smem32[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    uint32_t* wsm = smem32 + warp * R32_WARP_WORDS;
+    __shared__ FamTab tab;
+    const uint32_t ntasks = P.scr[Scratch::NTASKS + 7];
+    pdl_trigger();
+    load_tab(tab, P.scr, 7);
+    __syncthreads();
+    uint32_t next = 0;  // the next task index, fetched while the current task runs
+    if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 7, 1u);
+    for (;;) {
+        const uint32_t t = __shfl_sync(MI_FULL_MASK, next, 0);
+        if (t >= ntasks) break;
+        if (lane == 0) next = atomicAdd(P.scr + Scratch::QUEUE + 7, 1u);
+        rect32_task(P, decode_tab<7>(tab, t), wsm);
     }
     pdl_wait();  // complete only after the task kernel launched before it
 }
@@ -944,6 +969,7 @@ __global__ void __launch_bounds__(256, 3) k_rg_add(Params P) {
 
 constexpr size_t kNttSmem = ntt32::MulSmem<11>::WORDS32 * 4 + 64;
 constexpr size_t kClsSmem = size_t(8) * CLS_WARP_WORDS * 4;
+constexpr size_t kR32Smem = size_t(8) * R32_WARP_WORDS * 4;
 constexpr size_t kC64Smem = size_t(4) * C64_GROUP_WORDS * 4;
 
 std::mutex g_init_mu;
@@ -958,9 +984,10 @@ mi_status init_device() {
     // keys of each family in descending cost
     std::vector<uint16_t> order(K);
     for (int k = 0; k < K_NTT; ++k) order[KEY_NTT + k] = uint16_t(KEY_NTT + (K_NTT - 1 - k));
-    // classical keys by descending cost: 32-thread groups from 8 chunks down
-    // to 1, then groups of 16, 8, 4, 2, 1 threads (one chunk each)
+    // classical keys by descending cost: groups of 16, 8, 4, 2, 1 threads (one
+    // chunk each); 32-thread products from 8 chunks down to 1
     for (int k = 0; k < K_CLS; ++k) order[KEY_CLS + k] = uint16_t(KEY_CLS + (K_CLS - 1 - k));
+    for (int k = 0; k < K_R32; ++k) order[KEY_R32 + k] = uint16_t(KEY_R32 + (K_R32 - 1 - k));
     // the comb family, the most passes first
     const int comb[K_CMB] = {6, 5, 4, 3, 2, 1, 0};
     for (int k = 0; k < K_CMB; ++k) order[KEY_CMB + k] = uint16_t(KEY_CMB + comb[k]);
@@ -973,6 +1000,7 @@ mi_status init_device() {
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_ntt<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNttSmem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_classic, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kClsSmem)));
+    MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_r32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kR32Smem)));
     MI_CUDA_TRY(cudaFuncSetAttribute(k_rg_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kC64Smem)));
     g_init[dev] = true;
     return MI_OK;
@@ -1020,6 +1048,7 @@ mi_status ragged_launch(mi_ctx ctx, const mi_op* ops, uint32_t n_ops, const uint
     MI_CUDA_TRY(cudaGetLastError());
     MI_CUDA_TRY(launch_pdl(k_rg_ntt<1>, persistent_grid((const void*)k_rg_ntt<1>, kNttSmem), 256, kNttSmem, st, P));
     MI_CUDA_TRY(launch_pdl(k_rg_ntt<2>, persistent_grid((const void*)k_rg_ntt<2>, kNttSmem), 256, kNttSmem, st, P));
+    MI_CUDA_TRY(launch_pdl(k_rg_r32, persistent_grid((const void*)k_rg_r32, kR32Smem), 256, kR32Smem, st, P));
     MI_CUDA_TRY(launch_pdl(k_rg_classic, persistent_grid((const void*)k_rg_classic, kClsSmem), 256, kClsSmem, st, P));
     // 64-thread classical groups serve shorter operands of 129..256 limbs below the crossover
     if (P.ntt_min > 129)

@@ -20,8 +20,8 @@ constexpr uint32_t kPolyNttMin = 448;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257), and so do those from kRaggedNtt40Min
 // limbs whose NTT runs on 40-bit digits and three primes.
-constexpr uint32_t kRaggedNttMin = 112;
-constexpr uint32_t kRaggedNtt40Min = 96;
+constexpr uint32_t kRaggedNttMin = 128;
+constexpr uint32_t kRaggedNtt40Min = 112;
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32, 32, 64, 64};
