@@ -88,6 +88,8 @@ struct Field {
         return hi + __umulhi(m, p) + (lo != 0u ? 1u : 0u);
     }
     __device__ __forceinline__ uint32_t reduce(uint32_t x) const { return min(x, x - p); }
+    // [0, 4p) -> [0, 2p)
+    __device__ __forceinline__ uint32_t reduce2(uint32_t x) const { return min(x, x - p2); }
 };
 
 // Shared-memory word of residue index i: XOR of bits 2-4 with bits 5-7.  A
@@ -216,8 +218,13 @@ __device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, cons
 }
 
 // Inverse transform without the 1/L scaling (DIT).  In: stride-1 layout of a
-// bit-reversed spectrum; out: x[j] = residue t + L/8*j in natural order;
-// values in [0, 2p) throughout.
+// bit-reversed spectrum, values in [0, 2p); out: x[j] = residue t + L/8*j in
+// natural order, values in [0, 2p).  In between the values are kept in
+// [0, 4p) (Harvey's lazy butterflies): a butterfly brings its unmultiplied
+// input to [0, 2p) with one conditional subtraction, the Shoup product of the
+// other is in [0, 2p) for any 32-bit input, and both outputs u + v and
+// u - v + 2p stay below 4p < 2^32 -- two integer instructions per butterfly
+// fewer than reducing both outputs.
 template <int LG>
 __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const uint2* __restrict__ itw_all,
                                         const Field& f) {
@@ -226,26 +233,27 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
     const uint32_t t = threadIdx.x % P::NT;
     const uint2* __restrict__ itw = itw_all + TwLayout::base(LG);
     auto bf = [&](int j, int k, uint32_t e) {
-        const uint32_t u = x[j], v = f.shoup(x[k], __ldg(itw + e));
-        x[j] = f.add(u, v);
-        x[k] = f.sub(u, v);
+        const uint32_t u = f.reduce2(x[j]), v = f.shoup(x[k], __ldg(itw + e));
+        x[j] = u + v;
+        x[k] = u + f.p2 - v;
     };
     if constexpr (P::R > 0) {
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {  // twiddle 1
+        for (int j = 0; j < 8; j += 2) {  // twiddle 1; inputs in [0, 2p)
             const uint32_t u = x[j], v = x[j + 1];
-            x[j] = f.add(u, v);
-            x[j + 1] = f.sub(u, v);
+            x[j] = u + v;
+            x[j + 1] = u + f.p2 - v;
         }
         if constexpr (P::R == 2) {
             const uint2 w1 = __ldg(itw + TwLayout::quarter(LG));
 #pragma unroll
             for (int j = 0; j < 8; j += 4) {
-                const uint32_t u0 = x[j], v0 = x[j + 2], u1 = x[j + 1], v1 = f.shoup(x[j + 3], w1);
-                x[j] = f.add(u0, v0);
-                x[j + 2] = f.sub(u0, v0);
-                x[j + 1] = f.add(u1, v1);
-                x[j + 3] = f.sub(u1, v1);
+                const uint32_t u0 = f.reduce2(x[j]), v0 = f.reduce2(x[j + 2]);
+                const uint32_t u1 = f.reduce2(x[j + 1]), v1 = f.shoup(x[j + 3], w1);
+                x[j] = u0 + v0;
+                x[j + 2] = u0 + f.p2 - v0;
+                x[j + 1] = u1 + v1;
+                x[j + 3] = u1 + f.p2 - v1;
             }
         }
         exchange<LG, 1>(xs, sh, 1, P::d(P::NF - 1));
@@ -265,6 +273,8 @@ __device__ __forceinline__ void inverse(uint32_t (&x)[8], uint32_t* sh, const ui
         for (int j = 0; j < 4; ++j) bf(j, j + 4, e0 + d * j);
         if (k > 0) exchange<LG, 1>(xs, sh, d, P::d(k - 1));
     }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = f.reduce2(x[j]);
 }
 
 }  // namespace ntt32
