@@ -101,6 +101,7 @@ mi_status ntt_tables_create(NttTables* T) {
             const uint64_t li = host_invmod(uint64_t(1) << lg, p);
             P.ka_by_lg[q][lg - 8][0] = shoup_pair(li, p);
             P.ka_by_lg[q][lg - 8][1] = shoup_pair(host_mulmod(li, r32, p), p);
+            P.kb_by_lg[q][lg - 8] = shoup_pair(host_mulmod(li, r64, p), p);
         }
         P.kb[q][0] = shoup_pair(r32, p);
         P.kb[q][1] = shoup_pair(r64, p);

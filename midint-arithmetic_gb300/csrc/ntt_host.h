@@ -25,8 +25,9 @@ constexpr NttPrime30 kNttPrimes[5] = {
 struct NttMulParams {
     uint32_t p[5];
     uint32_t pinv[5];             // -p^-1 mod 2^32
-    uint2 ka_by_lg[5][5][2];      // a's conversion for L = 2^(8+i): (L^-1, 2^32 L^-1) mod p
-    uint2 kb[5][2];               // b's conversion: (2^32, 2^64) mod p
+    uint2 ka_by_lg[5][5][2];      // for L = 2^(8+i): (L^-1, 2^32 L^-1) mod p
+    uint2 kb[5][2];               // (2^32, 2^64) mod p
+    uint2 kb_by_lg[5][5];         // for L = 2^(8+i): 2^64 L^-1 mod p (with ka_by_lg[..][1], b's conversion)
     uint2 garner[10];             // p_k^-1 mod p_i, for i = 1..4, k = 0..i-1
     const uint2* tw[5];           // (w^e, companion), w of order 4096, in ntt32::TwLayout order
     const uint2* itw[5];          // (w^-e, companion), the same layout

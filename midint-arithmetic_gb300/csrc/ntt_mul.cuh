@@ -16,9 +16,9 @@
 // A product runs the mode with the fewest primes whose digits fit the same
 // power-of-two length (DM40 when at most 5/8 of it is filled, DM48 at most
 // 3/4): fewer primes, the same transforms per prime.  For each prime the
-// group converts a and b into the field (a scaled by 1/L, so the inverse
-// transform needs no scaling pass,
-// and b by 2^32, which the Montgomery pointwise product takes out again),
+// group converts a and b into the field (a unscaled, b scaled by 2^32 / L:
+// the Montgomery pointwise product takes out 2^32 and the inverse transform
+// needs no 1/L pass),
 // runs the two forward transforms in lockstep (shared twiddle loads and
 // barriers), multiplies pointwise in registers and runs the inverse
 // transform (ntt32.cuh), leaving the residues in shared memory.  It then
@@ -50,6 +50,14 @@ struct MulSmem {
 // (Shoup pairs).
 __device__ __forceinline__ uint32_t convert(uint64_t x, const Field& f, uint2 k0, uint2 k1) {
     return f.add(f.shoup(uint32_t(x), k0), f.shoup(uint32_t(x >> 32), k1));
+}
+
+// x mod p in [0, 2p) for a digit x = lo + hi 2^32 < 2^64, c32 the Shoup pair
+// of 2^32 mod p: lo is brought below 2p by two conditional subtractions of 2p
+// (lo < 2^32 < 6p), hi 2^32 by one Shoup product -- one product instead of
+// the two of convert() for the operand that takes no scaling.
+__device__ __forceinline__ uint32_t reduce_digit(uint32_t lo, uint32_t hi, const Field& f, uint2 c32) {
+    return f.add(f.reduce2(f.reduce2(lo)), f.shoup(hi, c32));
 }
 
 // Digit modes (see the top of this file).
@@ -180,19 +188,22 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
 #pragma unroll 1
     for (int q = 0; q < NP; ++q) {
         const Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
-        const uint2 ka0 = P.ka_by_lg[q][LG - 8][0], ka1 = P.ka_by_lg[q][LG - 8][1];
-        const uint2 kb0 = P.kb[q][0], kb1 = P.kb[q][1];
+        // a unscaled; b times 2^32 / L (the Montgomery pointwise product takes
+        // out 2^32, and the inverse transform needs no 1/L pass)
+        const uint2 c32 = P.kb[q][0];
+        const uint2 kb0 = P.ka_by_lg[q][LG - 8][1], kb1 = P.kb_by_lg[q][LG - 8];
         uint32_t x[2][8];  // a and b, transformed in lockstep
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
             if constexpr (DM == DM64) {
-                x[0][j] = (i < la) ? convert(__ldg(ar + i), f, ka0, ka1) : 0u;
+                const uint64_t da = i < la ? __ldg(ar + i) : 0ull;
+                x[0][j] = reduce_digit(uint32_t(da), uint32_t(da >> 32), f, c32);
                 x[1][j] = (i < lb) ? convert(__ldg(br + i), f, kb0, kb1) : 0u;
             } else {
                 const uint2 da = digit_at<DM>(ar, la, i);
                 const uint2 db = digit_at<DM>(br, lb, i);
-                x[0][j] = f.add(f.shoup(da.x, ka0), f.shoup(da.y, ka1));
+                x[0][j] = reduce_digit(da.x, da.y, f, c32);
                 x[1][j] = f.add(f.shoup(db.x, kb0), f.shoup(db.y, kb1));
             }
         }

@@ -68,6 +68,19 @@ __device__ __forceinline__ uint32_t digit_residue(const uint64_t* x, uint32_t m,
     }
 }
 
+// Residue of digit i of an m-limb operand, unscaled (c32: the Shoup pair of
+// 2^32 mod p).
+template <bool D48>
+__device__ __forceinline__ uint32_t digit_plain(const uint64_t* x, uint32_t m, uint32_t i, const Field& f, uint2 c32) {
+    if constexpr (D48) {
+        const uint2 d = digit48_any(reinterpret_cast<const uint32_t*>(x), 2 * m, i);
+        return ntt32::reduce_digit(d.x, d.y, f, c32);
+    } else {
+        const uint64_t v = i < m ? x[i] : 0ull;
+        return ntt32::reduce_digit(uint32_t(v), uint32_t(v >> 32), f, c32);
+    }
+}
+
 // dst[0..m) = (x * y + addend) mod 2^(64m) (SQ: y is x).  x, y and addend are
 // generic pointers to m u64 limbs (global or shared); addend may be null; dst
 // is global or shared and may alias neither x nor y.  Every thread of the
@@ -87,13 +100,11 @@ __device__ __forceinline__ void lo_product(const uint64_t* x, const uint64_t* y,
     for (int q = 0; q < np; ++q) {
         const Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
         if constexpr (SQ) {
-            // X = F(x); pointwise X * (X * 2^32/L) / 2^32 = X^2 / L.  Conversion
-            // by 1: Shoup pairs of 1 (companion floor(2^32/p) = floor((2^32-1)/p),
-            // p odd) and of 2^32 mod p (b's pair kb[q][0])
-            const uint2 k0 = make_uint2(1u, 0xffffffffu / P.p[q]), k1 = P.kb[q][0], ks = P.ka_by_lg[q][LG - 8][1];
+            // X = F(x); pointwise X * (X * 2^32/L) / 2^32 = X^2 / L
+            const uint2 c32 = P.kb[q][0], ks = P.ka_by_lg[q][LG - 8][1];
             uint32_t v[1][8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) v[0][j] = digit_residue<D48>(x, m, t + Pl::NT * j, f, k0, k1);
+            for (int j = 0; j < 8; ++j) v[0][j] = digit_plain<D48>(x, m, t + Pl::NT * j, f, c32);
             ntt32::forward<LG, 1>(v, sh, P.tw[q], f);
 #pragma unroll
             for (int j = 0; j < 8; ++j) v[0][j] = f.mont(v[0][j], f.shoup(v[0][j], ks));
@@ -101,12 +112,13 @@ __device__ __forceinline__ void lo_product(const uint64_t* x, const uint64_t* y,
 #pragma unroll
             for (int j = 0; j < 4; ++j) res[q * HALF + ntt32::swz(t + Pl::NT * j)] = f.reduce(v[0][j]);
         } else {
-            const uint2 ka0 = P.ka_by_lg[q][LG - 8][0], ka1 = P.ka_by_lg[q][LG - 8][1];
-            const uint2 kb0 = P.kb[q][0], kb1 = P.kb[q][1];
+            // x unscaled, y times 2^32 / L
+            const uint2 c32 = P.kb[q][0];
+            const uint2 kb0 = P.ka_by_lg[q][LG - 8][1], kb1 = P.kb_by_lg[q][LG - 8];
             uint32_t v[2][8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                v[0][j] = digit_residue<D48>(x, m, t + Pl::NT * j, f, ka0, ka1);
+                v[0][j] = digit_plain<D48>(x, m, t + Pl::NT * j, f, c32);
                 v[1][j] = digit_residue<D48>(y, m, t + Pl::NT * j, f, kb0, kb1);
             }
             ntt32::forward<LG, 2>(v, sh, P.tw[q], f);
