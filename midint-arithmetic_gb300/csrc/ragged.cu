@@ -316,12 +316,12 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
 
 // DM: the digit mode of the family (64-bit digits on five primes, 48-bit
 // on four, 40-bit on three: a kernel each, so that no digit mode's code
-// raises another's registers).  Two CTAs per SM at up to 128 registers: at
-// three (85 registers) the 48-bit products spilled 40-68 bytes at every
-// transform length, and the list ran 0.8 % slower (NTT band 0.896 against
-// 0.878 ms on the 200000-op list).
+// raises another's registers).  The 64-bit family runs three CTAs per SM at
+// up to 80 registers (no spills; NTT band of the 200000-op list 0.786 ->
+// 0.777 ms against two), the others two at up to 128: at three they spill
+// 200-250 bytes.
 template <int DM>
-__global__ void __launch_bounds__(256, 2) k_rg_ntt(Params P) {
+__global__ void __launch_bounds__(256, DM == ntt32::DM64 ? 3 : 2) k_rg_ntt(Params P) {
     constexpr int F = DM == ntt32::DM64 ? 0 : (DM == ntt32::DM48 ? 4 : 6);  // family
     constexpr int KEY0 = DM == ntt32::DM64 ? KEY_NTT : (DM == ntt32::DM48 ? KEY_N48 : KEY_N40);
     extern __shared__ __align__(16) uint32_t smem[];
