@@ -17,8 +17,10 @@
 // registers) at strides L/8, L/64, ... and one final radix-2 or radix-4 pass
 // on 8 consecutive residues; the inverse is decimation in time in the reverse
 // pass order (bit-reversed in, natural out).  Between passes the residues are
-// exchanged through shared memory with an XOR swizzle of 32-bit words that
-// keeps the passes free of bank conflicts (one 2-way exchange at L = 1024).
+// exchanged through shared memory in a padded layout (residue i at word
+// i + 4 floor(i/32)) that keeps the passes free of bank conflicts (one 2-way
+// layout at L = 1024) and whose word addresses are a per-thread base plus a
+// compile-time offset per residue.
 // The reference instead runs lg L radix-2 stages in shared memory with a
 // barrier per stage, after a bit-reversal permutation with a barrier per
 // element, and reads each twiddle from global memory (fft/ifft,
@@ -108,9 +110,29 @@ struct Plan {
     __device__ static __forceinline__ uint32_t idx(int d, uint32_t t, int j) {
         return (t / d) * 8 * d + (t % d) + d * j;
     }
+    // Exchange arrays: residue i at word i + 4 floor(i/32), so L + L/8 words.
+    // For the residues idx(d, t, j) of a thread in the layout of stride d the
+    // word is xbase(d, t) + xoff(d, j): floor(idx/32) splits into a part of t
+    // and a part of j for every power-of-two d.  The 32 lanes of a warp then
+    // touch 32 distinct banks for d != 2 (2-way at d = 2), and the quads of
+    // the d = 1 layout 8 distinct 16-byte slots per quarter warp.
+    static constexpr int LX = L + L / 8;
+    __device__ static __forceinline__ uint32_t xbase(int d, uint32_t t) {
+        if (d >= 32) return (t / d) * 9 * d + (t % d) + 4 * ((t % d) >> 5);
+        if (d == 16) return 144 * (t / 16) + (t % 16);
+        if (d == 8) return 72 * (t / 8) + (t % 8);
+        if (d == 4) return 36 * (t / 4) + (t % 4);
+        if (d == 2) return 16 * (t / 2) + (t % 2) + 4 * (t / 4);
+        return 8 * t + 4 * (t / 4);
+    }
+    __host__ __device__ static constexpr uint32_t xoff(int d, int j) {
+        return d >= 32 ? uint32_t(9 * d / 8 * j)
+                       : (d == 16 ? uint32_t(16 * j + 4 * (j / 2))
+                                  : (d == 8 ? uint32_t(8 * j + 4 * (j / 4)) : uint32_t(d * j)));
+    }
 };
 
-// Moves the thread's 8 residues of each of NA arrays (each with its own L
+// Moves the thread's 8 residues of each of NA arrays (each with its own LX
 // words of `sh`) from layout (stride) d_from to d_to through shared memory.
 // In a layout of stride d <= 32 the residues of a warp are the 256
 // consecutive words of its own block, so an exchange between two such
@@ -126,25 +148,26 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NA][8], uint32_t* sh, int
     if (local) __syncwarp(); else __syncthreads();
 #pragma unroll
     for (int q = 0; q < NA; ++q) {
-        uint32_t* s = sh + q * P::L;
+        uint32_t* s = sh + q * P::LX;
+        const uint32_t b = P::xbase(d_from, t);
         if (d_from == 1) {
 #pragma unroll
             for (int j = 0; j < 8; j += 4)
-                *reinterpret_cast<uint4*>(s + swz(P::idx(1, t, j))) =
-                    make_uint4(x[q][j], x[q][j + 1], x[q][j + 2], x[q][j + 3]);
+                *reinterpret_cast<uint4*>(s + b + j) = make_uint4(x[q][j], x[q][j + 1], x[q][j + 2], x[q][j + 3]);
         } else {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) s[swz(P::idx(d_from, t, j))] = x[q][j];
+            for (int j = 0; j < 8; ++j) s[b + P::xoff(d_from, j)] = x[q][j];
         }
     }
     if (local) __syncwarp(); else __syncthreads();
 #pragma unroll
     for (int q = 0; q < NA; ++q) {
-        const uint32_t* s = sh + q * P::L;
+        const uint32_t* s = sh + q * P::LX;
+        const uint32_t b = P::xbase(d_to, t);
         if (d_to == 1) {
 #pragma unroll
             for (int j = 0; j < 8; j += 4) {
-                const uint4 v = *reinterpret_cast<const uint4*>(s + swz(P::idx(1, t, j)));
+                const uint4 v = *reinterpret_cast<const uint4*>(s + b + j);
                 x[q][j] = v.x;
                 x[q][j + 1] = v.y;
                 x[q][j + 2] = v.z;
@@ -152,7 +175,7 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NA][8], uint32_t* sh, int
             }
         } else {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) x[q][j] = s[swz(P::idx(d_to, t, j))];
+            for (int j = 0; j < 8; ++j) x[q][j] = s[b + P::xoff(d_to, j)];
         }
     }
 }

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__((1 << LG) / 8)
     k_ntt32_raw(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ out,
                 NttMulParams P, int q, int conv) {
     using Pl = ntt32::Plan<LG>;
-    __shared__ __align__(16) uint32_t sh[2 * Pl::L];
+    __shared__ __align__(16) uint32_t sh[2 * Pl::LX];
     const uint32_t t = threadIdx.x;
     const ntt32::Field f{P.p[q], 2 * P.p[q], P.pinv[q]};
     if (!conv) {

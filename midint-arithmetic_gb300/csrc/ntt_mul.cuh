@@ -39,11 +39,11 @@ namespace mi {
 namespace ntt32 {
 
 // Shared memory of one group, in 32-bit words: exchange buffers of a and b
-// (2L) + five residue arrays (5L).
+// (2 Plan::LX) + five residue arrays (5L).
 template <int LG>
 struct MulSmem {
     static constexpr int L = 1 << LG;
-    static constexpr size_t WORDS32 = size_t(7) * L;
+    static constexpr size_t WORDS32 = size_t(2) * Plan<LG>::LX + size_t(5) * L;
 };
 
 // x*K mod p in [0, 2p) for a digit x < 2^64: K0 = K mod p, K1 = 2^32 K mod p
@@ -182,8 +182,8 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
     using Dg = Digits<DM>;
     constexpr int NP = Dg::NP;
     constexpr int SW = 11;  // digit-sum words: 8 limbs + 3 overflow, 6 + 2 or 5 + 1 (+ headroom)
-    uint32_t* sh = sm;               // exchange buffers of a and b (2L)
-    uint32_t* res = sm + 2 * Pl::L;  // res[q][slot], q < NP
+    uint32_t* sh = sm;                // exchange buffers of a and b (2 LX)
+    uint32_t* res = sm + 2 * Pl::LX;  // res[q][slot], q < NP
     const uint32_t t = threadIdx.x % Pl::NT;
 #pragma unroll 1
     for (int q = 0; q < NP; ++q) {
@@ -269,7 +269,7 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
         }
     }
     // the overflow words go to the right neighbour through the exchange buffer
-    uint64_t* ov = reinterpret_cast<uint64_t*>(sh);  // 3 x 8 bytes x L/8 threads: fits the 8L bytes of sh
+    uint64_t* ov = reinterpret_cast<uint64_t*>(sh);  // 3 x 8 bytes x L/8 threads: fits the 9L bytes of sh
     finish_block<Pl::NT, Dg::OUT, Dg::OVW>(s, ov, rr, rlen, t, scr);
     __syncthreads();  // sh and res are reused by the next call
 }

@@ -36,13 +36,13 @@ namespace {
 using ntt32::Field;
 using ntt32::Plan;
 
-// Shared memory of one CTA, in 32-bit words: exchange buffers (2L), the
+// Shared memory of one CTA, in 32-bit words: exchange buffers (2 LX), the
 // low-half residues of five primes (5 L/2), and the three intermediates T1,
 // T2, P3 (m u64 limbs each, at most L/2 limbs: L words each).
 template <int LG>
 struct PolySmem {
     static constexpr int L = 1 << LG;
-    static constexpr int SH = 0, RES = 2 * L, T1 = RES + 5 * L / 2, T2 = T1 + L, P3 = T2 + L;
+    static constexpr int SH = 0, RES = 2 * Plan<LG>::LX, T1 = RES + 5 * L / 2, T2 = T1 + L, P3 = T2 + L;
     static constexpr size_t WORDS32 = size_t(P3 + L);
 };
 
