@@ -632,9 +632,57 @@ __device__ __forceinline__ void rect32_task(const Params& P, const Task& tk, uin
     __syncwarp();  // the warp's area is reused by its next task
 }
 
+// The R x C-word product of A and B in one parity-split accumulator, as
+// classic::tile_mac does for 8 x 8 tiles: products with i + j even go to a
+// (pairs at even columns), those with i + j odd to b (column k + 1 at b[k]),
+// so every (lo, hi) pair is one wide multiply-add; each row is two carry
+// chains whose single carry-outs land in cc (column C + i at cc[i]).
+template <int R, int C>
+struct RectAcc {
+    uint32_t a[R + C], b[R + C - 2], cc[R + 1];
+};
+
+template <int R, int C>
+__device__ __forceinline__ void rect_mac(const uint32_t (&A)[R], const uint32_t (&B)[C], RectAcc<R, C>& s) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j0 = i & 1, j1 = 1 - j0;
+        mad_lo_cc(s.a[i + j0], A[i], B[j0]);
+        madc_hi_cc(s.a[i + j0 + 1], A[i], B[j0]);
+#pragma unroll
+        for (int j = j0 + 2; j < C; j += 2) {
+            madc_lo_cc(s.a[i + j], A[i], B[j]);
+            madc_hi_cc(s.a[i + j + 1], A[i], B[j]);
+        }
+        addc(s.cc[i + j0], 0u);
+        mad_lo_cc(s.b[i + j1 - 1], A[i], B[j1]);
+        madc_hi_cc(s.b[i + j1], A[i], B[j1]);
+#pragma unroll
+        for (int j = j1 + 2; j < C; j += 2) {
+            madc_lo_cc(s.b[i + j - 1], A[i], B[j]);
+            madc_hi_cc(s.b[i + j], A[i], B[j]);
+        }
+        addc(s.cc[i + j1], 0u);
+    }
+}
+
+// The R + C words of the product from its accumulator (which fits them).
+template <int R, int C>
+__device__ __forceinline__ void rect_fold(RectAcc<R, C>& s, uint32_t (&f)[R + C]) {
+#pragma unroll
+    for (int c = 0; c < R + C; ++c) f[c] = s.a[c];
+    add_cc(f[1], s.b[0]);
+#pragma unroll
+    for (int k = 1; k < R + C - 2; ++k) addc_cc(f[k + 1], s.b[k]);
+    addc(f[R + C - 1], 0u);
+    add_cc(f[C], s.cc[0]);
+#pragma unroll
+    for (int i = 1; i < R; ++i) addc_cc(f[C + i], s.cc[i]);
+}
+
 // Comb products, shorter operand y of at most 8 limbs (16 words, held in
 // registers by every thread of the group): thread t multiplies its 16 words
-// of the longer operand x by y (row carry chains in 64-bit arithmetic), keeps
+// of the longer operand x by y (one parity-split accumulator, rect_mac), keeps
 // the low 16 words and hands the high 16 to thread t+1, whose low words they
 // overlap; one carry-lookahead pass over the group makes 16 result words per
 // thread final, and the last thread's high words plus the carry-out open the
@@ -677,18 +725,16 @@ __device__ __forceinline__ void comb_task(const Params& P, const Task& tk) {
             a[i + 1] = v.y;
         }
         uint32_t acc[K + NBW];
+        {
+            RectAcc<K, NBW> ra;
 #pragma unroll
-        for (int w = 0; w < NBW; ++w) acc[w] = 0;
+            for (int w = 0; w < K + NBW; ++w) ra.a[w] = 0;
 #pragma unroll
-        for (int i = 0; i < K; ++i) {
-            uint64_t c = 0;
+            for (int w = 0; w < K + NBW - 2; ++w) ra.b[w] = 0;
 #pragma unroll
-            for (int j = 0; j < NBW; ++j) {
-                const uint64_t v = uint64_t(a[i]) * B[j] + acc[i + j] + c;  // < 2^64
-                acc[i + j] = uint32_t(v);
-                c = v >> 32;
-            }
-            acc[i + NBW] = uint32_t(c);
+            for (int w = 0; w <= K; ++w) ra.cc[w] = 0;
+            rect_mac<K, NBW>(a, B, ra);
+            rect_fold<K, NBW>(ra, acc);
         }
         // words [base, base + K): the low words plus the previous thread's
         // high words (the pending words for the group's first thread)
