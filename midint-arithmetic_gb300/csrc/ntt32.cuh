@@ -183,8 +183,10 @@ __device__ __forceinline__ void exchange(uint32_t (&x)[NA][8], uint32_t* sh, int
 // Forward transforms (DIF) of NA arrays in lockstep on one prime (each
 // twiddle is loaded once for all of them).  In: x[q][j] = residue t + L/8*j
 // (natural order), values in [0, 2p).  Out: layout stride 1 (x[q][j] = slot
-// 8t+j of the bit-reversed spectrum), values in [0, 2p).
-template <int LG, int NA>
+// 8t+j of the bit-reversed spectrum), values in [0, 2p).  HALF: residues
+// L/2.. are zero (x[q][4..7] are not read), so the first stage of the first
+// pass is x[j + 4] = x[j] w with x[j] unchanged.
+template <int LG, int NA, bool HALF = false>
 __device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, const uint2* __restrict__ tw_all,
                                         const Field& f) {
     using P = Plan<LG>;
@@ -204,8 +206,17 @@ __device__ __forceinline__ void forward(uint32_t (&x)[NA][8], uint32_t* sh, cons
         const int d = P::d(k);
         if (k > 0) exchange<LG, NA>(x, sh, P::d(k - 1), d);
         const uint32_t off = t % d, e0 = TwLayout::pass(LG, k) + off;
+        if (HALF && k == 0) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf(j, j + 4, e0 + d * j);
+            for (int j = 0; j < 4; ++j) {
+                const uint2 w = __ldg(tw + e0 + d * j);
+#pragma unroll
+                for (int q = 0; q < NA; ++q) x[q][j + 4] = f.shoup(x[q][j], w);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bf(j, j + 4, e0 + d * j);
+        }
 #pragma unroll
         for (int j = 0; j < 8; j += 4) {
             bf(j, j + 2, e0 + 4 * d);

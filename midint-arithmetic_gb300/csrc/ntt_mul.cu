@@ -53,7 +53,8 @@ __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     extern __shared__ __align__(16) uint32_t smem32[];
     uint32_t* scratch = smem32 + ntt32::MulSmem<LG>::WORDS32;
     for (uint64_t inst = blockIdx.x; inst < n; inst += gridDim.x)
-        ntt32::mul_one<LG, 5 - NP>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32, scratch);
+        ntt32::mul_one<LG, 5 - NP, true>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32,
+                                         scratch);  // L = pow2ceil(2m): both operands in the lower half
 }
 
 template <int LG, int NP>

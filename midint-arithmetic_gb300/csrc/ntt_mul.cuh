@@ -173,8 +173,12 @@ __device__ __forceinline__ void finish_block(const uint64_t (&s)[SW], uint64_t* 
 // the top coefficient, falls inside the OUT*L/8 limbs the group produces;
 // limbs beyond rlen are dropped.  `sm` is the group's MulSmem, `scr` per-warp
 // scratch of the block.  Every thread of the block must call this with the
-// same LG and DM (the exchanges synchronise the block).
-template <int LG, int DM>
+// same LG and DM (the exchanges synchronise the block).  HALF: both operands'
+// digits lie below L/2 (balanced products: L = pow2ceil(2m)), so the upper
+// half of each transform input is zero and is neither converted nor added
+// (a compile-time choice: as a run-time flag in the ragged tasks it cost more
+// than it saved).
+template <int LG, int DM, bool HALF = false>
 __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_t la, const uint64_t* __restrict__ br,
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
                                         uint32_t* sm, uint32_t* scr) {
@@ -196,6 +200,10 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const uint32_t i = t + Pl::NT * j;
+            if (HALF && j >= 4) {
+                x[0][j] = x[1][j] = 0u;
+                continue;
+            }
             if constexpr (DM == DM64) {
                 const uint64_t da = i < la ? __ldg(ar + i) : 0ull;
                 x[0][j] = reduce_digit(uint32_t(da), uint32_t(da >> 32), f, c32);
@@ -207,7 +215,7 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
                 x[1][j] = f.add(f.shoup(db.x, kb0), f.shoup(db.y, kb1));
             }
         }
-        forward<LG, 2>(x, sh, P.tw[q], f);
+        forward<LG, 2, HALF>(x, sh, P.tw[q], f);
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[0][j] = f.mont(x[0][j], x[1][j]);
         inverse<LG>(x[0], sh, P.itw[q], f);

@@ -104,8 +104,8 @@ __device__ __forceinline__ void lo_product(const uint64_t* x, const uint64_t* y,
             const uint2 c32 = P.kb[q][0], ks = P.ka_by_lg[q][LG - 8][1];
             uint32_t v[1][8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) v[0][j] = digit_plain<D48>(x, m, t + Pl::NT * j, f, c32);
-            ntt32::forward<LG, 1>(v, sh, P.tw[q], f);
+            for (int j = 0; j < 4; ++j) v[0][j] = digit_plain<D48>(x, m, t + Pl::NT * j, f, c32);
+            ntt32::forward<LG, 1, true>(v, sh, P.tw[q], f);  // m digits fit L/2: the upper half is zero
 #pragma unroll
             for (int j = 0; j < 8; ++j) v[0][j] = f.mont(v[0][j], f.shoup(v[0][j], ks));
             ntt32::inverse<LG>(v[0], sh, P.itw[q], f);
@@ -117,11 +117,11 @@ __device__ __forceinline__ void lo_product(const uint64_t* x, const uint64_t* y,
             const uint2 kb0 = P.ka_by_lg[q][LG - 8][1], kb1 = P.kb_by_lg[q][LG - 8];
             uint32_t v[2][8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < 4; ++j) {
                 v[0][j] = digit_plain<D48>(x, m, t + Pl::NT * j, f, c32);
                 v[1][j] = digit_residue<D48>(y, m, t + Pl::NT * j, f, kb0, kb1);
             }
-            ntt32::forward<LG, 2>(v, sh, P.tw[q], f);
+            ntt32::forward<LG, 2, true>(v, sh, P.tw[q], f);  // the upper halves are zero
 #pragma unroll
             for (int j = 0; j < 8; ++j) v[0][j] = f.mont(v[0][j], v[1][j]);
             ntt32::inverse<LG>(v[0], sh, P.itw[q], f);
