@@ -10,18 +10,18 @@ namespace mi {
 namespace tuned {
 
 // mi_mul_u64: square products of at least this many u64 limbs use the NTT.
-constexpr uint32_t kPlainNttMin = 160;
+constexpr uint32_t kPlainNttMin = 96;
 // mi_mul_lo_u64: low halves of products of at least this many u64 limbs come
 // from the NTT kernel (2049 = never).
 constexpr uint32_t kLoNttMin = 320;
 // mi_poly_u64: composites of at least this many u64 limbs run their four
 // products on the NTT (2049 = never).
-constexpr uint32_t kPolyNttMin = 448;
+constexpr uint32_t kPolyNttMin = 320;
 // Ragged runs: products whose shorter operand has at least this many u64
 // limbs use the NTT kernel (1..257), and so do those from kRaggedNtt40Min
 // limbs whose NTT runs on 40-bit digits and three primes.
-constexpr uint32_t kRaggedNttMin = 128;
-constexpr uint32_t kRaggedNtt40Min = 112;
+constexpr uint32_t kRaggedNttMin = 112;
+constexpr uint32_t kRaggedNtt40Min = 96;
 // Batched addition: bytes of each operand a thread owns (16, 32 or 64), by
 // size class c = ceil(log2(u64 limbs)), c = 0..12.
 constexpr uint8_t kAddThreadBytes[13] = {16, 16, 16, 16, 32, 32, 32, 32, 16, 32, 32, 64, 64};

@@ -101,8 +101,9 @@ def test_mul_ntt_maximal_coefficients(ctx, devmem, m):
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m), O.mul(a, b, m, True))
 
 
-@pytest.mark.parametrize("m", [1, 100, 255, 256, 700, 1024, 2048])
+@pytest.mark.parametrize("m", [1, 64, 95, 96, 97, 100, 159, 160, 255, 256, 700, 1024, 2048])
 def test_mul_dispatch_matches_oracle(ctx, devmem, m):
+    # either side of the tuned classical/NTT crossover of mi_mul_u64
     a, b = carry_stress(5, m, seed=m + 3)
     assert np.array_equal(gpu_mul_ntt(ctx, devmem, a, b, m, via="dispatch"), O.mul(a, b, m, True))
 
