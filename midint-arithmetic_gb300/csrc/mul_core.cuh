@@ -415,8 +415,9 @@ __device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restri
 // Threads without a mirror (t >= H, and t = (nb-1)/2 for odd nb) read the
 // zero block nb instead, which exists whenever they do.  On return thread t
 // holds output blocks t (ulo) and NH+t (uhi), fully carried; the carry out of
-// block NB-1 is dropped (the product mod 2^(32*T*NB)).
-template <int NH, int UNROLL = NH >= 16 ? 8 : 2>
+// block NB-1 is dropped (the product mod 2^(32*T*NB)).  PREFETCH: each step's
+// operands are read one step ahead (16 more registers), as in square_product.
+template <int NH, int UNROLL = NH >= 16 ? 8 : 2, bool PREFETCH = false>
 __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
                                             uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
                                             uint32_t nb = 2 * NH) {
@@ -431,17 +432,35 @@ __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, 
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
     const uint32_t H = (nb + 1) / 2;
     const bool mirror = t < H && t < nb - 1 - t;  // owns a second anti-diagonal
+    // the blocks of step k: A-block i, B-block j
+    auto blocks = [&](uint32_t k, uint32_t& i, uint32_t& j) {
+        const bool first = k <= t;
+        i = first ? k : k - t - 1;
+        j = first ? t - k : nb - k;
+        if (first ? t >= H : !mirror) i = nb;  // a zero block
+    };
+    uint4 na0, na1, nb0, nb1;  // step k+1's operands (PREFETCH)
+    if (PREFETCH) {
+        uint32_t i, j;
+        blocks(0, i, j);
+        na0 = gA4[i], na1 = gA4[NB + i], nb0 = gB4[j], nb1 = gB4[NB + j];
+    }
 #pragma unroll UNROLL
     for (uint32_t k = 0; k <= nb; ++k) {
-        const bool first = k <= t;
-        uint32_t i = first ? k : k - t - 1;
-        const uint32_t j = first ? t - k : nb - k;
-        if (first ? t >= H : !mirror) i = nb;  // a zero block
         uint32_t A[T], B[T];
-        const uint4 a0 = gA4[i];
-        const uint4 a1 = gA4[NB + i];
-        const uint4 b0 = gB4[j];
-        const uint4 b1 = gB4[NB + j];
+        uint4 a0, a1, b0, b1;
+        if (PREFETCH) {
+            a0 = na0, a1 = na1, b0 = nb0, b1 = nb1;
+            if (k < nb) {
+                uint32_t i, j;
+                blocks(k + 1, i, j);
+                na0 = gA4[i], na1 = gA4[NB + i], nb0 = gB4[j], nb1 = gB4[NB + j];
+            }
+        } else {
+            uint32_t i, j;
+            blocks(k, i, j);
+            a0 = gA4[i], a1 = gA4[NB + i], b0 = gB4[j], b1 = gB4[NB + j];
+        }
         A[0] = a0.x; A[1] = a0.y; A[2] = a0.z; A[3] = a0.w;
         A[4] = a1.x; A[5] = a1.y; A[6] = a1.z; A[7] = a1.w;
         B[0] = b0.x; B[1] = b0.y; B[2] = b0.z; B[3] = b0.w;
