@@ -310,8 +310,11 @@ __device__ __forceinline__ void ntt_task(const Params& P, const Task& tk, uint32
     const bool busy = g < tk.count;
     mi_op op{};
     if (busy) op = P.ops[sorted[tk.first + g]];
-    ntt32::mul_one<LG, DM>(P.in + op.a_off, op.la, P.in + op.b_off, op.lb, busy ? P.out + op.r_off : nullptr,
-                            op.la + op.lb, P.ntt, gsm, scr_warp);
+    // 64-bit digits on 2048 points: both operands (at most kMaxLimbs = 1024
+    // limbs) lie in the lower half, so the zero upper half is skipped
+    ntt32::mul_one<LG, DM, DM == ntt32::DM64 && (1u << LG) >= 2 * kMaxLimbs>(
+        P.in + op.a_off, op.la, P.in + op.b_off, op.lb, busy ? P.out + op.r_off : nullptr, op.la + op.lb, P.ntt, gsm,
+        scr_warp);
 }
 
 // DM: the digit mode of the family (64-bit digits on five primes, 48-bit
