@@ -46,22 +46,22 @@ struct NttShape {
 
 // 768 threads per SM: three 256-thread CTAs for 2048-point transforms (one
 // 512-thread CTA for 4096-point ones)
-template <int LG, int NP>
+template <int LG, int NP, bool LOW>
 __global__ void __launch_bounds__((1 << LG) / 8, 768 / ((1 << LG) / 8))
     k_ntt_mul(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t* __restrict__ r, uint32_t n,
               uint32_t m, uint32_t rlen, NttMulParams P) {
     extern __shared__ __align__(16) uint32_t smem32[];
     uint32_t* scratch = smem32 + ntt32::MulSmem<LG>::WORDS32;
     for (uint64_t inst = blockIdx.x; inst < n; inst += gridDim.x)
-        ntt32::mul_one<LG, 5 - NP, true>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32,
-                                         scratch);  // L = pow2ceil(2m): both operands in the lower half
+        ntt32::mul_one<LG, 5 - NP, true, LOW>(a + inst * m, m, b + inst * m, m, r + inst * rlen, rlen, P, smem32,
+                                              scratch);  // L = pow2ceil(2m): both operands in the lower half
 }
 
 template <int LG, int NP>
 mi_status launch_lg(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t n, uint32_t m, uint32_t rlen,
                     const NttMulParams& P, cudaStream_t st) {
     using S = NttShape<LG>;
-    auto kern = k_ntt_mul<LG, NP>;
+    auto kern = rlen <= m ? k_ntt_mul<LG, NP, true> : k_ntt_mul<LG, NP, false>;  // the low half alone
     MI_TRY(ensure_dyn_smem(kern, S::SMEM));
     int per_sm = 0;
     MI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::NT, S::SMEM));

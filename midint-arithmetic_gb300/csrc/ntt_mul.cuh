@@ -177,8 +177,10 @@ __device__ __forceinline__ void finish_block(const uint64_t (&s)[SW], uint64_t* 
 // digits lie below L/2 (balanced products: L = pow2ceil(2m)), so the upper
 // half of each transform input is zero and is neither converted nor added
 // (a compile-time choice: as a run-time flag in the ragged tasks it cost more
-// than it saved).
-template <int LG, int DM, bool HALF = false>
+// than it saved).  LOW: only the low half of the product is stored (rlen <=
+// the digits below L/2), which the coefficients below L/2 alone determine, so
+// only those are kept and recombined.
+template <int LG, int DM, bool HALF = false, bool LOW = false>
 __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_t la, const uint64_t* __restrict__ br,
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
                                         uint32_t* sm, uint32_t* scr) {
@@ -220,7 +222,7 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
         for (int j = 0; j < 8; ++j) x[0][j] = f.mont(x[0][j], x[1][j]);
         inverse<LG>(x[0], sh, P.itw[q], f);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = f.reduce(x[0][j]);
+        for (int j = 0; j < (LOW ? 4 : 8); ++j) res[q * Pl::L + swz(t + Pl::NT * j)] = f.reduce(x[0][j]);
     }
     __syncthreads();
 
@@ -233,6 +235,7 @@ __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_
     for (int w = 0; w < SW; ++w) s[w] = 0;
 #pragma unroll
     for (int j = 0; j < 8; j += 4) {
+        if (LOW && 8 * t >= Pl::L / 2) break;  // coefficients that reach no stored limb
         const uint32_t slot = swz(8 * t + j);  // the swizzle keeps the quad slot..slot+3 together
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
