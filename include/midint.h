@@ -411,6 +411,17 @@ mi_status mi_server_stats(mi_server server, uint64_t* batches, uint64_t* request
  * ------------------------------------------------------------------------- */
 mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s, double* seconds);
 
+/* Calibration of the host link as the zero-copy host-buffer calls use it:
+ * the SMs streaming `bytes` of mapped pinned host memory in 16-byte accesses
+ * -- reads of host_src, writes of host_dst, and a copy of bytes/2 from one to
+ * the other (both directions at once) -- in GB/s of bytes moved, best of 5.
+ * bytes a positive multiple of 32, both buffers 16-byte aligned, pinned and
+ * mapped (cudaHostAlloc under unified addressing).  The denominator of the
+ * end-to-end roofline.  Synchronous; current device.  No counterpart in the
+ * reference (its drivers copy with cudaMemcpy only). */
+mi_status mi_calib_host_link(const void* host_src, void* host_dst, size_t bytes, double* read_gbs,
+                             double* write_gbs, double* both_gbs);
+
 /* ---------------------------------------------------------------------------
  * One NTT on a single caller-chosen prime, in 64-bit Montgomery fields (a
  * separate radix-8 transform, csrc/ntt.cuh, that can run the reference's own
@@ -432,7 +443,7 @@ mi_status mi_ntt_raw(uint64_t p, uint64_t g, uint32_t two_adicity, uint32_t len,
  * of mi_ntt32_prime) with the context's resident twiddles: conv = 0 gives the
  * forward transform of `a` in natural order, X_k = sum_i a_i w^(ik) mod p with
  * w = g^((p-1)/len); conv = 1 the cyclic convolution of a and b mod p, by the
- * same per-prime steps as a multiplication (scaled conversions, lockstep
+ * same per-prime steps as a multiplication (b scaled by 2^32/L, lockstep
  * forward transforms, Montgomery pointwise product, inverse transform).
  * Replaces the role of the reference's fft / bmulFFTvalid
  * (cuda/ker-fft-mul.cu.h:304-348, 512-554) as the transform-level check.

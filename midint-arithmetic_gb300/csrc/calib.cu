@@ -42,6 +42,36 @@ __global__ void __launch_bounds__(256) k_imad_peak(uint32_t iters, uint32_t seed
     if (s == 0x9e3779b9u) out[0] = s;  // keeps the work observable
 }
 
+// Host-link streaming by the SMs over mapped pinned host memory (the access
+// pattern of the zero-copy host-buffer calls): 16-byte loads, stores, or a
+// copy, grid-strided over n 16-byte words.
+__global__ void __launch_bounds__(256) k_link_read(const uint4* __restrict__ p, size_t n, uint4* __restrict__ sink) {
+    uint4 x = make_uint4(0, 0, 0, 0);
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const uint4 v = __ldcs(p + i);
+        x.x ^= v.x, x.y ^= v.y, x.z ^= v.z, x.w ^= v.w;
+    }
+    if ((x.x & x.y & x.z & x.w) == 0xffffffffu) sink[0] = x;  // keeps the loads observable
+}
+__global__ void __launch_bounds__(256) k_link_write(uint4* __restrict__ p, size_t n) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        __stcs(p + i, make_uint4(uint32_t(i), 1u, 2u, 3u));
+}
+__global__ void __launch_bounds__(256) k_link_copy(const uint4* __restrict__ s, uint4* __restrict__ d, size_t n) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        __stcs(d + i, __ldcs(s + i));
+}
+
+// The device address of a mapped host buffer, or null.
+void* mapped(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 }  // namespace
 }  // namespace mi
 
@@ -73,5 +103,48 @@ extern "C" mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s,
     const double prods = double(blocks) * 256.0 * iters * kChains * kProdPerStep;
     *products_per_s = prods / (double(ms) * 1e-3);
     if (seconds) *seconds = double(ms) * 1e-3;
+    return MI_OK;
+}
+
+extern "C" mi_status mi_calib_host_link(const void* host_src, void* host_dst, size_t bytes, double* read_gbs,
+                                        double* write_gbs, double* both_gbs) {
+    if (host_src == nullptr || host_dst == nullptr || read_gbs == nullptr || write_gbs == nullptr ||
+        both_gbs == nullptr)
+        return set_error(MI_EINVAL, "calib_host_link: null pointer");
+    if (bytes < 32 || bytes % 32 != 0 || !aligned16(host_src) || !aligned16(host_dst))
+        return set_error(MI_EINVAL, "calib_host_link: bytes must be a positive multiple of 32 on 16-byte aligned buffers");
+    const uint4* src = static_cast<const uint4*>(mapped(host_src));
+    uint4* dst = static_cast<uint4*>(mapped(host_dst));
+    if (src == nullptr || dst == nullptr)
+        return set_error(MI_EINVAL, "calib_host_link: buffers must be pinned host memory mapped for the device");
+    const size_t n = bytes / 16;
+    const uint32_t blocks = uint32_t(sm_count() * 2);
+    uint4* sink = nullptr;
+    MI_CUDA_TRY(cudaMalloc(&sink, 16));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    cudaError_t err = cudaSuccess;
+    for (int it = 0; it < 6 && err == cudaSuccess; ++it) {  // the first round warms up
+        for (int k = 0; k < 3 && err == cudaSuccess; ++k) {
+            cudaEventRecord(e0);
+            if (k == 0) k_link_read<<<blocks, 256>>>(src, n, sink);
+            else if (k == 1) k_link_write<<<blocks, 256>>>(dst, n);
+            else k_link_copy<<<blocks, 256>>>(src, dst, n / 2);  // bytes/2 each way
+            cudaEventRecord(e1);
+            err = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (it > 0 && ms < best[k]) best[k] = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (err != cudaSuccess) return cuda_error(err, "calib_host_link kernel");
+    *read_gbs = double(bytes) / (double(best[0]) * 1e-3) / 1e9;
+    *write_gbs = double(bytes) / (double(best[1]) * 1e-3) / 1e9;
+    *both_gbs = double(bytes) / (double(best[2]) * 1e-3) / 1e9;
     return MI_OK;
 }

@@ -117,9 +117,9 @@ __global__ void k_ntt_raw(const uint64_t* __restrict__ a, const uint64_t* __rest
 // The transform code of the multiplication kernels (ntt32.cuh) on its own,
 // one block of L/8 threads: conv = 0 the forward transform of `a` (residues
 // < p) written in natural order, conv = 1 the cyclic convolution of a and b
-// mod p (a scaled by L^-1 and b by 2^32 with Shoup products, both forward
+// mod p (a as given, b scaled by 2^32 / L with a Shoup product, both forward
 // transforms in lockstep, the Montgomery pointwise product, the unscaled
-// inverse) -- exactly the per-prime steps of ntt32::mul_one.
+// inverse) -- exactly the per-prime steps of ntt32::mul_one on residues.
 template <int LG>
 __global__ void __launch_bounds__((1 << LG) / 8)
     k_ntt32_raw(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint32_t* __restrict__ out,
@@ -138,11 +138,11 @@ __global__ void __launch_bounds__((1 << LG) / 8)
         for (int j = 0; j < 8; ++j) out[__brev(8 * t + j) >> (32 - LG)] = f.reduce(x[0][j]);
         return;
     }
-    const uint2 ka = P.ka_by_lg[q][LG - 8][0], kb = P.kb[q][0];
+    const uint2 kb = P.ka_by_lg[q][LG - 8][1];  // 2^32 / L
     uint32_t x[2][8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        x[0][j] = f.shoup(a[t + Pl::NT * j], ka);
+        x[0][j] = a[t + Pl::NT * j];  // residues < p
         x[1][j] = f.shoup(b[t + Pl::NT * j], kb);
     }
     ntt32::forward<LG, 2>(x, sh, P.tw[q], f);

@@ -62,6 +62,8 @@ SIGNATURES = {
     "mi_host_add_u64": (_S, [_P, _P, _P, _P, _P, _U32, _U32]),
     "mi_host_mul_full_u64": (_S, [_P, _P, _P, _P, _U32, _U32]),
     "mi_calib_mul32_peak": (_S, [_U32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "mi_calib_host_link": (_S, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "mi_mul_ntt_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_poly_u64": (_S, [_P, _P, _P, _P, _U32, _U32, _P]),
     "mi_import_words": (_S, [_P, _P, _U32, _U32, _U32, _I, _I, _P, _U32, _P]),
@@ -361,6 +363,14 @@ def calib_mul32_peak(iters: int = 0) -> float:
     v, t = ctypes.c_double(), ctypes.c_double()
     check(load().mi_calib_mul32_peak(iters, ctypes.byref(v), ctypes.byref(t)))
     return v.value
+
+
+def calib_host_link(src, dst, nbytes: int) -> tuple[float, float, float]:
+    """SM-driven host-link rates over mapped pinned host buffers (pointers or
+    pinned tensors): (read, write, both directions) in GB/s."""
+    r, w, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(load().mi_calib_host_link(_ptr(src), _ptr(dst), nbytes, ctypes.byref(r), ctypes.byref(w), ctypes.byref(b)))
+    return r.value, w.value, b.value
 
 
 def ntt_raw(p: int, g: int, two_adicity: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:

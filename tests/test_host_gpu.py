@@ -233,3 +233,16 @@ def test_contexts_on_several_host_threads(lib):
     assert not errors, errors
     for o in outs:
         assert np.array_equal(o.numpy().view(np.uint64), want)
+
+
+def test_calib_host_link(ctx):
+    # SM-driven streaming over mapped pinned memory: plausible rates, and
+    # sizes that are not a multiple of 32 bytes refused before any launch
+    nb = 8 << 20
+    src = torch.empty(nb, dtype=torch.uint8).pin_memory()
+    dst = torch.empty(nb, dtype=torch.uint8).pin_memory()
+    r, w, b = midint.calib_host_link(src, dst, nb)
+    assert 1.0 < r < 5000.0 and 1.0 < w < 5000.0 and 1.0 < b < 10000.0
+    with pytest.raises(midint.MidintError) as e:
+        midint.calib_host_link(src, dst, nb - 16)
+    assert e.value.status == midint.MI_EINVAL
