@@ -29,7 +29,10 @@ template <int NT, bool WB = false>
 struct MulShape {
     static constexpr bool WARP = WB && (NT == 16 || NT == 32);  // one-warp blocks
     static constexpr int BLOCK = WARP ? 32 : (NT > 256 ? NT : 256);
-    static constexpr int MIN_BLOCKS = WARP ? 24 : (NT >= 512 ? 1 : (NT == 2 ? 2 : 3));
+    // one-warp blocks: 16 per SM for 32-thread groups (up to 128 registers, 114
+    // used: 0.1376 -> 0.1362 ms on the 8192-bit batch against 24 at 80; 20,
+    // 14 and 12 measured 0.1367, 0.1368 and 0.1428 ms), 24 for 16-thread groups
+    static constexpr int MIN_BLOCKS = WARP ? (NT == 32 ? 16 : 24) : (NT >= 512 ? 1 : (NT == 2 ? 2 : 3));
     static constexpr int IPB = BLOCK / NT;   // instances per block
     static constexpr int WPAD = NT * T;      // padded limbs per operand
     // operands (2 x IPB x WPAD words) + per-thread snapshot/combine words; the
