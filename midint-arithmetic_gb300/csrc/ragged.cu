@@ -19,16 +19,20 @@
 //       digits on four for the products whose 48-bit digits fit the same L,
 //       and one with 40-bit digits on three for those whose 40-bit digits
 //       fit it (and whose shorter operand stays within the 3-prime bound);
-//     * classical products with a shorter operand of 9 to 128 limbs, a task
-//       per warp: 32/NT products whose shorter operand fits NT tiles of 8 u32
-//       limbs, broadcast to the group, while the longer one streams through
-//       in chunks of NT tiles, each chunk a square product (mul_core.cuh)
-//       whose carry pass also adds the pending window of the chunk before,
-//       the low half final -- no padding of either operand to a power of two;
+//     * classical products with a shorter operand of 9 to 128 limbs whose
+//       wider operand exceeds 16 tiles of 8 u32 limbs: one warp per product
+//       over rounds of 32 output blocks (rect32_task), the shorter operand
+//       broadcast, the longer one in chunks of 32 tiles in two alternating
+//       shared-memory buffers, one anti-diagonal per lane per round and a
+//       snapshot only in the first (wrap-around) round;
+//     * the narrower ones (both operands within 16 tiles): a task per warp
+//       of 32/NT square products (mul_core.cuh) whose shorter operand is the
+//       broadcast side -- no padding of either operand to a power of two;
 //     * comb products, shorter operand of at most 8 limbs, a family and a
 //       kernel of their own (each thread multiplies 16 words of the longer
-//       operand by all of the shorter one in registers);
-//     * the same chunked products for 129..256 limbs in 64-thread groups;
+//       operand by all of the shorter one in one parity-split accumulator);
+//     * chunked square products for 129..256 limbs in 64-thread groups, each
+//       chunk's carry pass adding the pending window of the chunk before;
 //     * additions, a task per warp: lanes of one limb for additions of up to
 //       32 limbs, rows of 32 limbs per warp above that.
 // Within a family the key encodes everything that sets the trip counts of a
@@ -369,11 +373,12 @@ __device__ __forceinline__ void load_chunk_regs(uint4 (&q)[classic::T / 4], cons
     }
 }
 
-// One classical task: NT <= 32, 32/NT groups in the caller's warp (`sm` is the
-// warp's area, the groups interleaved); NT = 64, the four 64-thread groups of
-// the block (`sm` the block's area, one C64_GROUP_WORDS region per group;
-// groups without a product run on zeros so the block's barriers match, `scr`
-// holds the block's per-warp carry words).
+// One classical task: NT <= 16, 32/NT groups in the caller's warp, one chunk
+// (`sm` is the warp's area, the groups interleaved); NT = 64, the four
+// 64-thread groups of the block, one or more chunks (`sm` the block's area,
+// one C64_GROUP_WORDS region per group; groups without a product run on zeros
+// so the block's barriers match, `scr` holds the block's per-warp carry
+// words).
 template <int NT>
 __device__ __forceinline__ void classic_task(const Params& P, const Task& tk, uint32_t* sm, uint32_t* scr) {
     using classic::T;
