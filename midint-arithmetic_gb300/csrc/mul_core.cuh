@@ -244,9 +244,10 @@ __device__ __forceinline__ void stage_b(uint4* gB4, const uint32_t* __restrict__
 // flight per step), shallow where registers are short (small groups, the
 // ragged kernel's interleaved groups).
 //
-// PREFETCH: the operands of step k+1 are read from shared memory into
-// registers before the tile of step k is multiplied (16 more registers), so a
-// warp's multiply-adds never wait for its own loads.
+// PREFETCH: the operands of steps k+1 and k+2 are read from shared memory
+// into registers before the tile of step k is multiplied (32 more registers),
+// so a warp's multiply-adds never wait for its own loads (two steps ahead
+// against one: 0.1362 -> 0.1355 ms on the 8192-bit batch, 124 registers).
 //
 // alo: when given, T more words added to the thread's output block t (lo)
 // in the same carry pass (the ragged products' pending window).
@@ -264,11 +265,19 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
     for (int w = 0; w < T + 1; ++w) s.cc[w] = 0;
     const uint32_t snap_k = t < nb ? t : nb - 1;
     uint4 na0, na1, nb0, nb1;  // step k+1's operands (PREFETCH)
+    uint4 ma0, ma1, mb0, mb1;  // step k+2's (nb >= 2 whenever PREFETCH is used)
     if (PREFETCH) {
         na0 = reinterpret_cast<const uint4*>(gA)[0];
         na1 = reinterpret_cast<const uint4*>(gA)[1];
         nb0 = gB4[t & uint32_t(NT - 1)];
         nb1 = gB4[G * NT + (t & uint32_t(NT - 1))];
+        if (nb > 1) {
+            const uint32_t jn = (t - 1) & uint32_t(NT - 1);
+            ma0 = reinterpret_cast<const uint4*>(gA + G * T)[0];
+            ma1 = reinterpret_cast<const uint4*>(gA + G * T)[1];
+            mb0 = gB4[jn];
+            mb1 = gB4[G * NT + jn];
+        }
     }
 #pragma unroll UNROLL
     for (uint32_t k = 0; k < nb; ++k) {
@@ -277,12 +286,13 @@ __device__ __forceinline__ void square_product(const uint32_t* gA, const uint4* 
         uint4 a0, a1, b0, b1;
         if (PREFETCH) {
             a0 = na0, a1 = na1, b0 = nb0, b1 = nb1;
-            if (k + 1 < nb) {
-                const uint32_t jn = (t - k - 1) & uint32_t(NT - 1);
-                na0 = reinterpret_cast<const uint4*>(gA + (k + 1) * G * T)[0];
-                na1 = reinterpret_cast<const uint4*>(gA + (k + 1) * G * T)[1];
-                nb0 = gB4[jn];
-                nb1 = gB4[G * NT + jn];
+            na0 = ma0, na1 = ma1, nb0 = mb0, nb1 = mb1;
+            if (k + 2 < nb) {
+                const uint32_t jn = (t - k - 2) & uint32_t(NT - 1);
+                ma0 = reinterpret_cast<const uint4*>(gA + (k + 2) * G * T)[0];
+                ma1 = reinterpret_cast<const uint4*>(gA + (k + 2) * G * T)[1];
+                mb0 = gB4[jn];
+                mb1 = gB4[G * NT + jn];
             }
         } else {
             a0 = reinterpret_cast<const uint4*>(gA + k * G * T)[0];
@@ -416,7 +426,7 @@ __device__ __forceinline__ void stage_planes(uint4* g4, const uint32_t* __restri
 // zero block nb instead, which exists whenever they do.  On return thread t
 // holds output blocks t (ulo) and NH+t (uhi), fully carried; the carry out of
 // block NB-1 is dropped (the product mod 2^(32*T*NB)).  PREFETCH: each step's
-// operands are read one step ahead (16 more registers), as in square_product.
+// operands are read one step ahead (16 more registers).
 template <int NH, int UNROLL = NH >= 16 ? 8 : 2, bool PREFETCH = false>
 __device__ __forceinline__ void low_product(const uint4* gA4, const uint4* gB4, uint2* slots, uint32_t* scr,
                                             uint32_t t, uint32_t (&ulo)[T], uint32_t (&uhi)[T],
