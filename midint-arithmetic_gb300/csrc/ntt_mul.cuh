@@ -177,9 +177,9 @@ __device__ __forceinline__ void finish_block(const uint64_t (&s)[SW], uint64_t* 
 // digits lie below L/2 (balanced products: L = pow2ceil(2m)), so the upper
 // half of each transform input is zero and is neither converted nor added
 // (a compile-time choice: as a run-time flag in the ragged tasks it cost more
-// than it saved).  LOW: only the low half of the product is stored (rlen <=
-// the digits below L/2), which the coefficients below L/2 alone determine, so
-// only those are kept and recombined.
+// than it saved).  LOW: only the low half of a balanced product is stored
+// (rlen at most m limbs, all of them below digit L/2); the coefficients below
+// L/2 alone determine those limbs, so only they are kept and recombined.
 template <int LG, int DM, bool HALF = false, bool LOW = false>
 __device__ __forceinline__ void mul_one(const uint64_t* __restrict__ ar, uint32_t la, const uint64_t* __restrict__ br,
                                         uint32_t lb, uint64_t* __restrict__ rr, uint32_t rlen, const NttMulParams& P,
