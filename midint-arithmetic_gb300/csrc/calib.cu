@@ -93,7 +93,8 @@ extern "C" mi_status mi_calib_mul32_peak(uint32_t iters, double* products_per_s,
     cudaEventRecord(e0);
     k_imad_peak<<<blocks, 256>>>(iters, 2u, d_out);
     cudaEventRecord(e1);
-    cudaError_t err = cudaEventSynchronize(e1);
+    cudaError_t err = cudaGetLastError();  // a failed launch would leave an empty timed region
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
@@ -133,7 +134,8 @@ extern "C" mi_status mi_calib_host_link(const void* host_src, void* host_dst, si
             else if (k == 1) k_link_write<<<blocks, 256>>>(dst, n);
             else k_link_copy<<<blocks, 256>>>(src, dst, n / 2);  // bytes/2 each way
             cudaEventRecord(e1);
-            err = cudaEventSynchronize(e1);
+            err = cudaGetLastError();
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
             if (it > 0 && ms < best[k]) best[k] = ms;
