@@ -32,7 +32,11 @@ struct MulShape {
     // one-warp blocks: 16 per SM for 32-thread groups (up to 128 registers, 114
     // used: 0.1376 -> 0.1362 ms on the 8192-bit batch against 24 at 80; 20,
     // 14 and 12 measured 0.1367, 0.1368 and 0.1428 ms), 24 for 16-thread groups
-    static constexpr int MIN_BLOCKS = WARP ? (NT == 32 ? 16 : 24) : (NT >= 512 ? 1 : (NT == 2 ? 2 : 3));
+    // 256-thread blocks of 16- or 32-thread groups serve only the capped
+    // zero-copy launches (two resident blocks per SM there), whose groups keep
+    // the next instance's operands in registers
+    static constexpr int MIN_BLOCKS = WARP ? (NT == 32 ? 16 : 24)
+                                           : (NT >= 512 ? 1 : (NT == 2 || NT == 16 || NT == 32 ? 2 : 3));
     static constexpr int IPB = BLOCK / NT;   // instances per block
     static constexpr int WPAD = NT * T;      // padded limbs per operand
     // operands (2 x IPB x WPAD words) + per-thread snapshot/combine words; the
@@ -62,14 +66,52 @@ __global__ void __launch_bounds__(MulShape<NT, WB>::BLOCK, MulShape<NT, WB>::MIN
     pdl_wait();  // launched with launch_pdl
     pdl_trigger();
 
+    if constexpr ((NT == 16 || NT == 32) && !S::WARP && VEC) {
+        if (full && n32 == NT * T) {
+            // The capped launches of the zero-copy host path, whose rows are
+            // host-mapped: each group reads the operands of its next instance
+            // into registers while it multiplies this one, and its product
+            // leaves through the group's operand areas as stores of whole
+            // 16-byte slots in order (one contiguous 16*NT-byte run per warp
+            // instruction rather than every other slot).  0.250 -> 0.240 ms for
+            // the 8192-bit batch of 16384 products over the host link.
+            uint4 qa[T / 4], qb[T / 4];
+            uint64_t inst = uint64_t(blockIdx.x) * S::IPB + grp;
+            classic::fetch_ab<NT, true>(qa, qb, a + inst * n32, b + inst * n32, n32, inst < n, t);
+            uint4* gA4 = reinterpret_cast<uint4*>(gA);
+            for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride, inst += stride) {
+                classic::put_ab<NT>(gA, gB4, qa, qb, t);
+                group_sync<NT>();
+                const uint64_t next = inst + stride;
+                classic::fetch_ab<NT, true>(qa, qb, a + next * n32, b + next * n32, n32, next < n, t);
+                uint32_t ulo[T], uhi[T];
+                classic::square_product<NT, 1, NT, false>(gA, gB4, slots, scr, t, ulo, uhi, NT);
+                if (inst < n) {
+                    group_sync<NT>();  // the group's operand reads are done
+                    gA4[2 * t] = make_uint4(ulo[0], ulo[1], ulo[2], ulo[3]);
+                    gA4[2 * t + 1] = make_uint4(ulo[4], ulo[5], ulo[6], ulo[7]);
+                    gB4[2 * t] = make_uint4(uhi[0], uhi[1], uhi[2], uhi[3]);
+                    gB4[2 * t + 1] = make_uint4(uhi[4], uhi[5], uhi[6], uhi[7]);
+                    group_sync<NT>();
+                    uint4* r4 = reinterpret_cast<uint4*>(r + inst * rlen);  // 4*NT slots
+                    __stcs(r4 + t, gA4[t]);
+                    __stcs(r4 + NT + t, gA4[NT + t]);
+                    __stcs(r4 + 2 * NT + t, gB4[t]);
+                    __stcs(r4 + 3 * NT + t, gB4[NT + t]);
+                }
+                group_sync<NT>();  // shared memory is reused by the next instance
+            }
+            return;
+        }
+    }
+
     // Every group of a block runs the same trip count (wide groups synchronise
     // the whole block).
     for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride) {
         const uint64_t inst = base + grp;
         const bool valid = inst < n;
         const uint64_t off = valid ? inst * n32 : 0;
-        classic::stage_a<NT, VEC>(gA, a + off, n32, valid, t);
-        classic::stage_b<NT, VEC>(gB4, b + off, n32, valid, t);
+        classic::stage_ab<NT, VEC>(gA, gB4, a + off, b + off, n32, valid, t);
         group_sync<NT>();
         uint32_t ulo[T], uhi[T];
         if (nb == NT)  // no padding: a compile-time trip count, unrolled in full for 8..32 steps; the

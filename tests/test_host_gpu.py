@@ -124,12 +124,30 @@ def test_zero_copy_with_capped_occupancy(hctx, blocks):
     hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 1)
     hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, blocks)
     assert hctx.get_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1) == blocks
-    for n, m in ((1500, 128), (37, 5), (64, 512)):
+    for n, m in ((1500, 128), (999, 64), (37, 5), (64, 512)):
         a, b = carry_stress(n, m, seed=blocks * 100 + m)
         pa, pb = _pinned(a), _pinned(b)
         pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
         hctx.host_mul_full(pa, pb, pr, n, m)
         assert np.array_equal(pr.numpy().view(np.uint64), O.mul(a, b, m, True))
+    hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, 0)
+
+
+@pytest.mark.parametrize("m", [64, 128])
+def test_zero_copy_strides_over_a_large_batch(hctx, m):
+    """Mode 1 on a batch larger than the capped grid (32 blocks per SM of
+    256 threads): each group reads its next instance's operands while it
+    multiplies the current one, over several rounds and a ragged last one."""
+    hctx.set_tuning(midint.TUNE_HOST_ZERO_COPY, 1, 1)
+    hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, 2)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    per_block = 256 // (m // 4)  # instances of one 256-thread block (groups of m/4 threads)
+    n = sms * 32 * per_block + 777
+    a, b = carry_stress(n, m, seed=m + 5)
+    pa, pb = _pinned(a), _pinned(b)
+    pr = torch.zeros(2 * n * m, dtype=torch.int64).pin_memory()
+    hctx.host_mul_full(pa, pb, pr, n, m)
+    assert np.array_equal(pr.numpy().view(np.uint64), O.mul(a, b, m, True))
     hctx.set_tuning(midint.TUNE_HOST_ZC_BLOCKS, 1, 0)
 
 
