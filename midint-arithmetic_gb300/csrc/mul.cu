@@ -29,9 +29,9 @@ template <int NT, bool WB = false>
 struct MulShape {
     static constexpr bool WARP = WB && (NT == 16 || NT == 32);  // one-warp blocks
     static constexpr int BLOCK = WARP ? 32 : (NT > 256 ? NT : 256);
-    // one-warp blocks: 16 per SM for 32-thread groups (up to 128 registers, 114
-    // used: 0.1376 -> 0.1362 ms on the 8192-bit batch against 24 at 80; 20,
-    // 14 and 12 measured 0.1367, 0.1368 and 0.1428 ms), 24 for 16-thread groups
+    // one-warp blocks: 16 per SM for 32-thread groups (up to 128 registers:
+    // 0.1376 -> 0.1362 ms on the 8192-bit batch against 24 at 80; 20, 14 and
+    // 12 measured 0.1367, 0.1368 and 0.1428 ms), 24 for 16-thread groups;
     // 256-thread blocks of 16- or 32-thread groups serve only the capped
     // zero-copy launches (two resident blocks per SM there), whose groups keep
     // the next instance's operands in registers
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(MulShape<NT, WB>::BLOCK, MulShape<NT, WB>::MIN
             // into registers while it multiplies this one, and its product
             // leaves through the group's operand areas as stores of whole
             // 16-byte slots in order (one contiguous 16*NT-byte run per warp
-            // instruction rather than every other slot).  0.250 -> 0.240 ms for
+            // instruction rather than every other slot).  0.250 -> 0.242 ms for
             // the 8192-bit batch of 16384 products over the host link.
             uint4 qa[T / 4], qb[T / 4];
             uint64_t inst = uint64_t(blockIdx.x) * S::IPB + grp;
