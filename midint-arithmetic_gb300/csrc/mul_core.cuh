@@ -228,8 +228,10 @@ __device__ __forceinline__ void put_ab(uint32_t* gA, uint4* gB4, const uint4 (&q
 
 // Stages both operand rows of a group.  All loads are issued before the first
 // shared-memory store, so the group waits for one round trip to memory, not
-// one per operand -- what counts over host-mapped rows (the zero-copy host
-// path: 0.264 -> 0.250 ms for the 8192-bit batch of 16384 products).
+// one per operand -- what counts over host-mapped rows: it took the zero-copy
+// host step of the 8192-bit batch of 16384 products from 0.264 to 0.250 ms
+// (that launch shape now has a loop of its own in k_mul, on the same two
+// halves, fetch_ab and put_ab).
 template <int NT, bool VEC>
 __device__ __forceinline__ void stage_ab(uint32_t* gA, uint4* gB4, const uint32_t* __restrict__ ra,
                                          const uint32_t* __restrict__ rb, uint32_t n32, bool valid, uint32_t t) {
