@@ -184,7 +184,6 @@ mi_status ensure_stage(mi_ctx ctx, size_t bytes) {
     return MI_OK;
 }
 
-// The device address of a mapped pinned host buffer, or null.
 // The device address of a mapped pinned host buffer that kernels may read or
 // write in place, or null.  Buffers that are not 8-byte aligned are not used
 // in place (the staging buffers of the copy path are): the u64 and NTT
