@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(MulShape<NT, WB>::BLOCK, MulShape<NT, WB>::MIN
             for (uint64_t base = uint64_t(blockIdx.x) * S::IPB; base < n; base += stride, inst += stride) {
                 classic::put_ab<NT>(gA, gB4, qa, qb, t);
                 group_sync<NT>();
-                const uint64_t next = inst + stride;
+                const uint64_t next = inst + stride;  // past the batch: nothing is read (valid = false)
                 classic::fetch_ab<NT, true>(qa, qb, a + next * n32, b + next * n32, n32, next < n, t);
                 uint32_t ulo[T], uhi[T];
                 classic::square_product<NT, 1, NT, false>(gA, gB4, slots, scr, t, ulo, uhi, NT);
